@@ -1,0 +1,321 @@
+"""Benchmark: L1 pdist of 100,000 float32 PCFs (L ~ Poisson(256) + 2,
+N(0,1) values, last value 0, Exp(1) gaps) on one GB300.
+
+A step is one full pdist pass over the whole problem (4,999,950,000 pairs)
+with the CSR input and the 20 GB condensed output resident in HBM.
+Prints one JSON line (see the keys below).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n N]
+
+``--impl reference`` times the reference's CPU algorithm (the oracle's C
+restatement of stablebear's CPU pairwise task, all host threads) on bounded
+row samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PCF pairs/s, L1 pdist N=100k fp32, 1 GB300"
+UNIT = "pairs/s"
+W_SEG = 5  # algorithmic FP32 lane-ops per merged segment (compare, dt, diff, scale, accumulate)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=100_000, help="PCFs (the benchmark workload is 100000)")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample-rows", type=int, default=0, help="rows in the CPU baseline sample (0 = auto)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(n, seed):
+    from stablebear_gb300 import synthetic
+    pts, off = synthetic.large_l1(n, seed=seed)
+    return pts, off
+
+
+def config(args, n, ws):
+    return {"workload": f"L1 pdist, N={n} float32 PCFs, L~Poisson(256)+2, N(0,1) values, Exp(1) gaps, seed=0",
+            "n_pcfs": n, "pairs_per_step": n * (n - 1) // 2,
+            "output": "condensed DistanceMatrix float32 kept in HBM",
+            "l2": "inputs (CSR) and output larger than L2; no flush",
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
+
+
+def sample_rows(n, target_pairs, seed=1):
+    """Rows spread over the whole triangle whose partner counts sum to about
+    target_pairs (row i has i partners in the lower triangle)."""
+    rng = np.random.default_rng(seed)
+    k = max(1, int(target_pairs / max(1, n / 2)))
+    rows = np.unique(rng.integers(1, n, size=k)).astype(np.uint64)
+    return rows
+
+
+def cpu_baseline(pts, off, rows, threads):
+    from oracle import oracle as orc
+    t0 = time.perf_counter()
+    vals, starts = orc.evaluate_rows(pts, off, rows, op=orc.OP_L1, mode=orc.MODE_PDIST, threads=threads)
+    dt = time.perf_counter() - t0
+    pairs = int(starts[-1])
+    return pairs / dt, dt, pairs, vals, starts
+
+
+# ---- clocks --------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, mx, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        load = [s for s in sm if mx and s > 0.3 * mx] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+# ---- reference arm ---------------------------------------------------------------
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    pts, off = workload(args.n, seed=0)
+    threads = os.cpu_count() or 1
+    rows = sample_rows(args.n, 2.0e6 if args.n >= 50_000 else args.n * (args.n - 1) / 2)
+    for _ in range(args.warmup):
+        cpu_baseline(pts, off, rows[: max(1, len(rows) // 8)], threads)
+    rates, times, pairs_tot = [], [], 0
+    for _ in range(args.steps):
+        r, dt, pairs, _, _ = cpu_baseline(pts, off, rows, threads)
+        rates.append(r)
+        times.append(dt)
+        pairs_tot += pairs
+    value = pairs_tot / sum(times)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config(args, args.n, ws),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{len(rows)} rows of the N={args.n} triangle "
+                                       f"({pairs_tot // max(1, args.steps)} pairs per step), "
+                                       "oracle C restatement of the reference CPU task, all host threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+# ---- GPU arm -------------------------------------------------------------------
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import stablebear_gb300 as sb
+    from stablebear_gb300 import _native as nat, synthetic
+
+    n = args.n
+    pts, off = workload(n, seed=rank)
+    lens = np.diff(off.astype(np.int64))
+    lmax = int(lens.max())
+    pairs = n * (n - 1) // 2
+    segs = synthetic.segment_count(off, pts, 1)
+
+    dev = torch.device("cuda", local)
+    dp = torch.from_numpy(pts).to(dev)
+    do = torch.from_numpy(off.astype(np.int64)).to(dev)
+    out = torch.empty(pairs, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    lib = nat.lib()
+
+    def step():
+        nat.check(lib.sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                          do.data_ptr(), n, None, None, 0, None, None, lmax, out.data_ptr(), 0, 0, 0,
+                                          sptr))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for k in range(args.steps):
+        step()
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    per = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = ws * pairs * args.steps / (total_ms / 1e3)
+
+    # parity on sampled rows of the device result against the oracle
+    parity = None
+    cpu = None
+    rows = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        target = args.cpu_sample_rows * n / 2 if args.cpu_sample_rows else 6.0e6 * threads / 16
+        rows = sample_rows(n, target)
+        rate, dt, npairs, vals, starts = cpu_baseline(pts, off, rows, threads)
+        host = out.cpu().numpy() if pairs <= 6_000_000_000 else None
+        got = np.concatenate([host[int(i) * (int(i) - 1) // 2: int(i) * (int(i) - 1) // 2 + int(i)] for i in rows])
+        rel = np.abs(got.astype(np.float64) - vals) / np.maximum(np.abs(vals.astype(np.float64)), 1e-30)
+        from oracle import oracle as orc
+        trows = rows[:: max(1, len(rows) // 12)]
+        tv, _ = orc.evaluate_rows(pts, off, trows, truth=True, threads=threads)
+        gt = np.concatenate([host[int(i) * (int(i) - 1) // 2: int(i) * (int(i) - 1) // 2 + int(i)] for i in trows])
+        relt = np.abs(gt.astype(np.float64) - tv) / np.maximum(np.abs(tv), 1e-30)
+        parity = {"rows_checked": int(len(rows)), "pairs_checked": int(npairs),
+                  "max_rel_err_vs_reference_cpu": float(rel.max()),
+                  "max_rel_err_vs_fp64_oracle": float(relt.max()), "tolerance": 1e-5,
+                  "ok": bool(rel.max() <= 1e-5 and relt.max() <= 1e-5)}
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{len(rows)} random rows of the same N={n} triangle, {npairs} pairs, {dt:.1f} s; "
+                         "oracle C restatement of the reference CPU pairwise task"}
+        del host
+
+    # end to end through the public C ABI with host buffers
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        hout = np.empty(pairs, dtype=np.float32)
+        hout[::262144] = 0  # touch pages outside the timed region
+        hout[:] = 0
+        offs = np.ascontiguousarray(off)
+
+        def e2e_step():
+            nat.check(lib.sbg_pairwise_host(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, nat.ptr(pts),
+                                            nat.ptr(offs), n, None, None, 0, nat.ptr(hout), 0))
+
+        e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        dt = (time.perf_counter() - t0) / args.e2e_steps
+        e2e = {"value": pairs / dt, "unit": UNIT, "h2d_bytes_per_step": int(pts.nbytes + offs.nbytes),
+               "d2h_bytes_per_step": int(hout.nbytes), "ms_per_step": dt * 1e3, "steps": args.e2e_steps,
+               "api": "sbg_pairwise_host (host CSR in, host DistanceMatrix storage out)"}
+        del hout
+
+    # roofline of the pair kernel: FP32 issue rate
+    from stablebear_gb300 import roofline
+    peak = roofline.fp32_peak(local)
+    achieved = segs * W_SEG / (ms_step / 1e3) / 1e12
+    traffic = roofline.traffic_per_launch("pairs_kernel_l1_f32", n)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": config(args, n, ws),
+        "segments_per_s": segs * ws / (ms_step / 1e3), "segments_per_step": segs,
+        "roofline": {"bound": "fp32_issue", "achieved": achieved, "peak": peak["value"], "unit": "T lane-op/s",
+                     "frac": achieved / peak["value"], "traffic": traffic, "peak_source": peak["source"],
+                     "work_model": f"{W_SEG} FP32 lane-ops per merged segment x {segs} segments per launch"},
+        "hbm_output_stream": {"bytes_per_launch": pairs * 4, "achieved_gbs": pairs * 4 / (ms_step / 1e3) / 1e9},
+        "clocks": clk, "gpu_launches": args.steps, "step_ms": per,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if parity:
+        line["parity"] = parity
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

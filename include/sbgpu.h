@@ -1,0 +1,188 @@
+/*
+ * sbgpu.h — C ABI of the GB300 pairwise-integration engine for arrays of
+ * piecewise constant functions (PCFs): Lp distance matrices (pdist / cdist,
+ * p >= 1) and L2 kernel (Gram) matrices.
+ *
+ * Plain C: pointers, sizes and status codes; no exceptions cross it.  Every
+ * entry point returns SBG_OK (0) or a negative sbg_status; sbg_last_error()
+ * then holds a message for the calling thread.
+ *
+ * Input layout (all entry points): the reference's CSR of SimplePoint
+ * (include/sbear/cuda/offset_data_manager.hpp:42-68,
+ *  include/sbear/cuda/cuda_matrix_integrate_structs.cuh:9-14):
+ *   points  — interleaved (t, v) pairs of the element type, PCF i at
+ *             points[2*offsets[i] .. 2*offsets[i+1])
+ *   offsets — n + 1 uint64 values, offsets[0] == 0.
+ * Each PCF starts at t = 0 with non-decreasing, finite times
+ * (src/python/pypcf_support.hpp:76-89); host entry points check this.
+ *
+ * Output layouts are the reference's:
+ *   DistanceMatrix (pdist):  n(n-1)/2 values, (i, j), i > j at i(i-1)/2 + j
+ *                            (include/sbear/distance_matrix.hpp:141-146)
+ *   SymmetricMatrix (kernel): n(n+1)/2 values, (i, j), i >= j at i(i+1)/2 + j
+ *                            (include/sbear/symmetric_matrix.hpp:248-260)
+ *   dense (cdist):           n_rows x n_cols row-major
+ *                            (include/sbear/cuda/cuda_result_writer.hpp:17-34)
+ */
+#ifndef SBGPU_H
+#define SBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SBG_API_VERSION 1
+
+typedef enum sbg_status {
+  SBG_OK = 0,
+  SBG_ERR_INVALID_ARGUMENT = -1,
+  SBG_ERR_INVALID_INPUT = -2,   /* input violates the PCF contract */
+  SBG_ERR_CUDA = -3,            /* "file:line: <cuda message>" (cuda_util.cuh:8-10) */
+  SBG_ERR_OUT_OF_MEMORY = -4,
+  SBG_ERR_CANCELLED = -5,       /* request_stop() ended the task */
+  SBG_ERR_NO_DEVICE = -6,
+  SBG_ERR_TIMEOUT = -7,
+  SBG_ERR_INTERNAL = -8,
+  SBG_ERR_LOGIC = -9            /* logic_error (cuda_result_writer.hpp:63-90) */
+} sbg_status;
+
+typedef enum sbg_dtype { SBG_F32 = 0, SBG_F64 = 1 } sbg_dtype;
+
+/* Pair operations (include/sbear/functional/operations.cuh:19-65). */
+typedef enum sbg_op { SBG_OP_L1 = 0, SBG_OP_LP = 1, SBG_OP_L2_INNER = 2 } sbg_op;
+
+/* Which pairs / which layout; values equal the reference's TriangleSkipMode
+ * (include/sbear/cuda/triangle_skip_mode.hpp:7-12). */
+typedef enum sbg_skip_mode {
+  SBG_SKIP_NONE = 0,           /* cdist: all pairs, dense row-major */
+  SBG_SKIP_LOWER_NODIAG = 1,   /* pdist: i > j, DistanceMatrix order */
+  SBG_SKIP_LOWER = 2           /* l2 kernel: i >= j, SymmetricMatrix order */
+} sbg_skip_mode;
+
+/* ---- library --------------------------------------------------------------- */
+
+int sbg_api_version(void);
+/* Message of the last failing call on this thread ("" if none). */
+const char* sbg_last_error(void);
+/* "CUDA" — this build has no CPU path (pymodule.cpp: _build_type). */
+const char* sbg_build_type(void);
+/* Number of visible CUDA devices (pymodule.cpp: get_ngpus). */
+int sbg_get_ngpus(int* n);
+
+/* ---- settings: sb::Settings (include/sbear/settings.hpp:8-23) and the
+ *      setters bound in src/python/pymodule.cpp:136-151 ------------------------ */
+
+int sbg_set_force_cpu(int on);            /* accepted; this build always runs on the GPU */
+int sbg_get_force_cpu(void);
+int sbg_set_cuda_threshold(uint64_t n);   /* accepted; no CPU path to fall back to */
+uint64_t sbg_get_cuda_threshold(void);
+int sbg_set_block_dim(unsigned x, unsigned y);
+int sbg_set_min_block_side(uint64_t n);
+int sbg_limit_gpus(int n);
+int sbg_limit_cpus(int n);
+int sbg_set_device_verbose(int on);
+int sbg_get_device_verbose(void);
+/* Engine knobs (0 = automatic): warps per CTA, rows per work item / 32,
+ * variant (1 shared-memory, 2 global-memory), order (1 caller's, 2 sorted
+ * by breakpoint count), output bytes per pipeline band. */
+int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes);
+
+/* ---- tasks: the 12 factories of include/sbear/cuda/cuda_matrix_integrate_api.hpp:19-113
+ *      and StoppableTask (include/sbear/task.hpp:15-172) ------------------------ */
+
+typedef struct sbg_task sbg_task;
+
+/* pdist (skip_mode SBG_SKIP_LOWER_NODIAG, out = DistanceMatrix storage) or
+ * l2 kernel (SBG_SKIP_LOWER, out = SymmetricMatrix storage) of one PCF set.
+ * Replaces create_cuda_block_integrate_{l1,lp,l2_kernel}_task
+ * (cuda_matrix_integrate_api.hpp:19-63).  The PCFs are copied into the task
+ * (as pcf_block_op.cuh:143 copies them); `out` is caller-owned host memory
+ * that must outlive the task.  op SBG_OP_LP takes p >= 1. */
+int sbg_create_integrate_task(int dtype, int op, double p, int skip_mode,
+                              const void* points, const uint64_t* offsets, uint64_t n,
+                              void* out, sbg_task** task);
+
+/* cdist between two PCF sets into a dense n_rows x n_cols host matrix.
+ * Replaces create_cuda_block_cdist_{l1,lp,l2_kernel}_task
+ * (cuda_matrix_integrate_api.hpp:67-113). */
+int sbg_create_cdist_task(int dtype, int op, double p,
+                          const void* row_points, const uint64_t* row_offsets, uint64_t n_rows,
+                          const void* col_points, const uint64_t* col_offsets, uint64_t n_cols,
+                          void* out, sbg_task** task);
+
+/* StoppableTask::start_async (task.hpp:43-49): runs on a worker thread. */
+int sbg_task_start(sbg_task* task);
+/* StoppableTask::wait_for (task.hpp:84-96): *finished = 0 while running,
+ * 1 once done; the worker's error status is returned once, on the call that
+ * observes completion. */
+int sbg_task_wait_for(sbg_task* task, int64_t timeout_ms, int* finished);
+/* StoppableTask::wait (task.hpp:98-107). */
+int sbg_task_wait(sbg_task* task);
+/* StoppableTask::request_stop / stop_requested (task.hpp:21-31). */
+int sbg_task_request_stop(sbg_task* task);
+int sbg_task_stop_requested(const sbg_task* task);
+/* work_total / work_completed / work_step (task.hpp:51-64). */
+int sbg_task_progress(const sbg_task* task, uint64_t* work_total, uint64_t* work_completed, uint64_t* work_step);
+/* work_step_desc / work_step_unit (task.hpp:66-76), NUL-terminated into buf. */
+int sbg_task_step_text(const sbg_task* task, char* desc, size_t desc_cap, char* unit, size_t unit_cap);
+/* Waits for a running task, then frees it. */
+void sbg_task_destroy(sbg_task* task);
+
+/* ---- synchronous host-buffer entry (blocking; what the task runs) --------- */
+
+/* skip_mode as above; col_* ignored unless skip_mode == SBG_SKIP_NONE.
+ * validate != 0 checks the input contract first. */
+int sbg_pairwise_host(int dtype, int op, double p, int skip_mode,
+                      const void* row_points, const uint64_t* row_offsets, uint64_t n_rows,
+                      const void* col_points, const uint64_t* col_offsets, uint64_t n_cols,
+                      void* out, int validate);
+
+/* ---- stream-ordered device entry --------------------------------------------
+ * All pointers are device pointers on the current device; work is enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream).  out_base is
+ * subtracted from every output index (a caller writing rows
+ * [row_begin, row_end) of a condensed matrix into a band buffer passes the
+ * band's first index); row_end = 0 means all rows.  max_points is the largest
+ * breakpoint count over rows and columns (0: measured on the device, which
+ * synchronises the stream).  row_perm / col_perm (optional, uint32) give the
+ * processing order; results always land at the callers' (i, j).  Inputs are
+ * not validated; malformed times cannot make the kernel read out of bounds. */
+int sbg_pairwise_device(int dtype, int op, double p, int skip_mode,
+                        const void* row_points, const uint64_t* row_offsets, uint64_t n_rows,
+                        const void* col_points, const uint64_t* col_offsets, uint64_t n_cols,
+                        const uint32_t* row_perm, const uint32_t* col_perm, uint32_t max_points,
+                        void* out, uint64_t out_base, uint64_t row_begin, uint64_t row_end,
+                        void* stream);
+
+/* The persistent kernel's work items for rows [row_begin, row_end) of a
+ * problem with 32*q rows per item: writes (chunk, column group) pairs for
+ * item ids 0.. into out (2*cap uint64) and returns the item count.  Host-only
+ * (no device needed); used by tests and tooling to check that the items tile
+ * the requested triangle or rectangle exactly once. */
+uint64_t sbg_enumerate_items(int skip_mode, uint64_t n_rows, uint64_t n_cols, uint64_t row_begin,
+                             uint64_t row_end, uint32_t q, uint64_t* out, uint64_t cap);
+
+/* Measured issue rate of the current device for the roofline: kind 0 =
+ * FP32 FFMA, 1 = FP64 DFMA, in lane-operations per second (one FMA
+ * instruction per lane = one lane-op), from a register-only FMA loop. */
+int sbg_measure_peak(int kind, double* lane_ops_per_s);
+
+/* Number of output elements of a problem (n(n-1)/2, n(n+1)/2 or n_rows*n_cols). */
+uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols);
+
+#ifdef __cplusplus
+}
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#endif /* SBGPU_H */

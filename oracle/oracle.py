@@ -1,0 +1,266 @@
+"""ORACLE — test infrastructure only (ctypes front-end of ``pcf_oracle.c``).
+
+Used by ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s
+CPU-baseline leg as the checker.  The product package never imports it.
+
+Inputs use the reference's CSR layout: ``points`` is an ``(M, 2)`` array of
+``(t, v)`` rows (float32 or float64), ``offsets`` a ``uint64`` array of length
+``N + 1``; PCF ``i`` is ``points[offsets[i]:offsets[i+1]]``
+(``include/sbear/cuda/offset_data_manager.hpp:42-68`` in the reference).
+
+Modes follow the reference's TriangleSkipMode
+(``include/sbear/cuda/triangle_skip_mode.hpp:7-12``): 0 = cdist (dense),
+1 = pdist (DistanceMatrix order), 2 = l2 kernel (SymmetricMatrix order).
+Ops follow ``include/sbear/functional/operations.cuh``: 0 = L1, 1 = Lp,
+2 = L2 inner product.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_oracle as _build
+
+OP_L1, OP_LP, OP_L2 = 0, 1, 2
+MODE_CROSS, MODE_PDIST, MODE_KERNEL = 0, 1, 2
+
+_lib = None
+_ref = None
+_P = ctypes.c_void_p
+_U64 = ctypes.c_uint64
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        lib = ctypes.CDLL(path)
+        lib.sbo_evaluate.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                     _P, _P, _U64, _P, _P, _U64, _P, ctypes.c_int]
+        lib.sbo_evaluate.restype = ctypes.c_int
+        lib.sbo_evaluate_rows.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                          _P, _P, _U64, _P, _P, _U64, _P, _U64, _P, _P, ctypes.c_int]
+        lib.sbo_evaluate_rows.restype = ctypes.c_int
+        lib.sbo_integrate_f32.argtypes = [_P, _U64, _P, _U64, ctypes.c_int, ctypes.c_float]
+        lib.sbo_integrate_f32.restype = ctypes.c_float
+        lib.sbo_integrate_f64.argtypes = [_P, _U64, _P, _U64, ctypes.c_int, ctypes.c_double]
+        lib.sbo_integrate_f64.restype = ctypes.c_double
+        lib.sbo_finalize_f32.argtypes = [ctypes.c_int, ctypes.c_float, ctypes.c_float]
+        lib.sbo_finalize_f32.restype = ctypes.c_float
+        lib.sbo_finalize_f64.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double]
+        lib.sbo_finalize_f64.restype = ctypes.c_double
+        lib.sbo_integrate_dd_f32.argtypes = [_P, _U64, _P, _U64, ctypes.c_int, ctypes.c_double]
+        lib.sbo_integrate_dd_f32.restype = ctypes.c_double
+        lib.sbo_integrate_dd_f64.argtypes = [_P, _U64, _P, _U64, ctypes.c_int, ctypes.c_double]
+        lib.sbo_integrate_dd_f64.restype = ctypes.c_double
+        lib.sbo_count_total_segments.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, _U64, _P, _P, _U64]
+        lib.sbo_count_total_segments.restype = _U64
+        _lib = lib
+    return _lib
+
+
+def ref_lib():
+    """The reference's own headers compiled into a shared library, or None
+    where the reference tree is absent."""
+    global _ref
+    if _ref is None:
+        try:
+            path = _build.build_ref()
+        except Exception:  # pragma: no cover - compiler problems mean "unavailable"
+            path = None
+        if path is None:
+            _ref = False
+        else:
+            lib = ctypes.CDLL(path)
+            lib.sbref_pair_f32.argtypes = [_P, _U64, _P, _U64, ctypes.c_int, ctypes.c_float]
+            lib.sbref_pair_f32.restype = ctypes.c_float
+            lib.sbref_pair_f64.argtypes = [_P, _U64, _P, _U64, ctypes.c_int, ctypes.c_double]
+            lib.sbref_pair_f64.restype = ctypes.c_double
+            lib.sbref_pairwise_f32.argtypes = [_P, _P, _U64, ctypes.c_int, ctypes.c_float, ctypes.c_int, _P]
+            lib.sbref_pairwise_f32.restype = ctypes.c_int
+            lib.sbref_pairwise_f64.restype = ctypes.c_int
+            lib.sbref_pairwise_f64.argtypes = [_P, _P, _U64, ctypes.c_int, ctypes.c_double, ctypes.c_int, _P]
+            lib.sbref_cross_f32.argtypes = [_P, _P, _U64, _P, _P, _U64, ctypes.c_int, ctypes.c_float, _P]
+            lib.sbref_cross_f64.argtypes = [_P, _P, _U64, _P, _P, _U64, ctypes.c_int, ctypes.c_double, _P]
+            lib.sbref_rectangles_f64.argtypes = [_P, _U64, _P, _U64, ctypes.c_double, ctypes.c_double, _P, _U64]
+            lib.sbref_rectangles_f64.restype = _U64
+            lib.sbref_schedule.argtypes = [_U64, _U64, _U64, _U64, ctypes.c_int, _U64, _P, _U64, _P, _P]
+            lib.sbref_schedule.restype = _U64
+            lib.sbref_subdivide.argtypes = [_U64, _U64, _P, _U64]
+            lib.sbref_subdivide.restype = _U64
+            _ref = lib
+    return _ref or None
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _dtype_code(points):
+    if points.dtype == np.float32:
+        return 0
+    if points.dtype == np.float64:
+        return 1
+    raise TypeError(f"unsupported dtype {points.dtype}")
+
+
+def _csr(points, offsets):
+    points = np.ascontiguousarray(points)
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    if points.ndim != 2 or points.shape[1] != 2:
+        raise ValueError("points must be (M, 2)")
+    return points, offsets
+
+
+def out_size(mode, n_rows, n_cols=None):
+    if mode == MODE_PDIST:
+        return n_rows * (n_rows - 1) // 2
+    if mode == MODE_KERNEL:
+        return n_rows * (n_rows + 1) // 2
+    return n_rows * n_cols
+
+
+def evaluate(points, offsets, *, op=OP_L1, p=1.0, mode=MODE_PDIST, col_points=None, col_offsets=None,
+             truth=False, threads=None):
+    """Naive restatement (``truth=False``; result in the input precision) or
+    the double-double truth oracle (``truth=True``; result float64)."""
+    lib = _load()
+    points, offsets = _csr(points, offsets)
+    dt = _dtype_code(points)
+    nr = len(offsets) - 1
+    if mode == MODE_CROSS:
+        col_points, col_offsets = _csr(col_points, col_offsets)
+        if col_points.dtype != points.dtype:
+            raise TypeError("row and column PCFs must share a dtype")
+        nc = len(col_offsets) - 1
+    else:
+        col_points, col_offsets, nc = points, offsets, nr
+    odt = np.float64 if truth else points.dtype
+    out = np.zeros(out_size(mode, nr, nc), dtype=odt)
+    if threads is None:
+        threads = os.cpu_count() or 1
+    lib.sbo_evaluate(dt, 1 if truth else 0, op, float(p), mode, _ptr(points), _ptr(offsets), nr,
+                     _ptr(col_points), _ptr(col_offsets), nc, _ptr(out), int(threads))
+    return out
+
+
+def evaluate_rows(points, offsets, rows, *, op=OP_L1, p=1.0, mode=MODE_PDIST, truth=False, threads=None,
+                  col_points=None, col_offsets=None):
+    """Evaluate only the listed rows.  Returns (values, row_starts) where row
+    ``rows[k]``'s results occupy ``values[row_starts[k]:row_starts[k+1]]``
+    (columns 0..i-1 for pdist, 0..i for the kernel, all for cdist)."""
+    lib = _load()
+    points, offsets = _csr(points, offsets)
+    dt = _dtype_code(points)
+    nr = len(offsets) - 1
+    rows = np.ascontiguousarray(rows, dtype=np.uint64)
+    if mode == MODE_CROSS:
+        col_points, col_offsets = _csr(col_points, col_offsets)
+        nc = len(col_offsets) - 1
+        counts = np.full(len(rows), nc, dtype=np.uint64)
+    else:
+        col_points, col_offsets, nc = points, offsets, nr
+        counts = rows + (1 if mode == MODE_KERNEL else 0)
+    starts = np.zeros(len(rows) + 1, dtype=np.uint64)
+    np.cumsum(counts, out=starts[1:])
+    odt = np.float64 if truth else points.dtype
+    out = np.zeros(int(starts[-1]), dtype=odt)
+    if threads is None:
+        threads = os.cpu_count() or 1
+    base = np.ascontiguousarray(starts[:-1])
+    lib.sbo_evaluate_rows(dt, 1 if truth else 0, op, float(p), mode, _ptr(points), _ptr(offsets), nr,
+                          _ptr(col_points), _ptr(col_offsets), nc, _ptr(rows), len(rows), _ptr(base),
+                          _ptr(out), int(threads))
+    return out, starts
+
+
+def pair(f, g, *, op=OP_L1, p=1.0, truth=False):
+    """One finalized pair value; ``f``/``g`` are (L, 2) arrays of one dtype."""
+    lib = _load()
+    f = np.ascontiguousarray(f)
+    g = np.ascontiguousarray(g)
+    if truth:
+        fn = lib.sbo_integrate_dd_f32 if f.dtype == np.float32 else lib.sbo_integrate_dd_f64
+        pp = float(np.float32(p)) if f.dtype == np.float32 else float(p)
+        return float(fn(_ptr(f), len(f), _ptr(g), len(g), op, pp))
+    if f.dtype == np.float32:
+        v = lib.sbo_integrate_f32(_ptr(f), len(f), _ptr(g), len(g), op, float(p))
+        return float(np.float32(lib.sbo_finalize_f32(op, float(p), v)))
+    v = lib.sbo_integrate_f64(_ptr(f), len(f), _ptr(g), len(g), op, float(p))
+    return float(lib.sbo_finalize_f64(op, float(p), v))
+
+
+def count_segments(points, offsets, mode=MODE_PDIST, col_points=None, col_offsets=None):
+    """Rectangles the reference's merge emits over the whole problem
+    (counted pair by pair; small problems only)."""
+    lib = _load()
+    points, offsets = _csr(points, offsets)
+    if mode == MODE_CROSS:
+        col_points, col_offsets = _csr(col_points, col_offsets)
+        nc = len(col_offsets) - 1
+    else:
+        col_points, col_offsets, nc = points, offsets, len(offsets) - 1
+    return int(lib.sbo_count_total_segments(_dtype_code(points), mode, _ptr(points), _ptr(offsets),
+                                            len(offsets) - 1, _ptr(col_points), _ptr(col_offsets), nc))
+
+
+# --- the reference's own code (where the reference tree is present) -----------
+
+def ref_evaluate(points, offsets, *, op=OP_L1, p=1.0, mode=MODE_PDIST, col_points=None, col_offsets=None):
+    lib = ref_lib()
+    if lib is None:
+        raise RuntimeError("reference harness unavailable (reference tree absent)")
+    points, offsets = _csr(points, offsets)
+    nr = len(offsets) - 1
+    f32 = points.dtype == np.float32
+    if mode == MODE_CROSS:
+        col_points, col_offsets = _csr(col_points, col_offsets)
+        nc = len(col_offsets) - 1
+        out = np.zeros(nr * nc, dtype=points.dtype)
+        fn = lib.sbref_cross_f32 if f32 else lib.sbref_cross_f64
+        fn(_ptr(points), _ptr(offsets), nr, _ptr(col_points), _ptr(col_offsets), nc, op, float(p), _ptr(out))
+        return out
+    out = np.zeros(out_size(mode, nr), dtype=points.dtype)
+    fn = lib.sbref_pairwise_f32 if f32 else lib.sbref_pairwise_f64
+    if fn(_ptr(points), _ptr(offsets), nr, op, float(p), mode, _ptr(out)) != 0:
+        raise ValueError("the reference container rejected a value")
+    return out
+
+
+def ref_rectangles(f, g, a=0.0, b=None):
+    lib = ref_lib()
+    if lib is None:
+        raise RuntimeError("reference harness unavailable (reference tree absent)")
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    if b is None:
+        b = np.finfo(np.float64).max
+    cap = 4 * (len(f) + len(g) + 4)
+    out = np.zeros(4 * cap, dtype=np.float64)
+    n = lib.sbref_rectangles_f64(_ptr(f), len(f), _ptr(g), len(g), float(a), float(b), _ptr(out), cap)
+    return out[: 4 * n].reshape(n, 4)
+
+
+def ref_schedule(n_rows, n_cols, max_out, n_splits, lower, min_side):
+    lib = ref_lib()
+    if lib is None:
+        raise RuntimeError("reference harness unavailable (reference tree absent)")
+    cap = 1 << 20
+    out = np.zeros(5 * cap, dtype=np.uint64)
+    mh = np.zeros(1, dtype=np.uint64)
+    mw = np.zeros(1, dtype=np.uint64)
+    n = lib.sbref_schedule(n_rows, n_cols, max_out, n_splits, 1 if lower else 0, min_side, _ptr(out), cap,
+                           _ptr(mh), _ptr(mw))
+    return out[: 5 * n].reshape(n, 5), int(mh[0]), int(mw[0])
+
+
+def ref_subdivide(block, n_items):
+    lib = ref_lib()
+    if lib is None:
+        raise RuntimeError("reference harness unavailable (reference tree absent)")
+    cap = n_items + 4
+    out = np.zeros(2 * cap, dtype=np.uint64)
+    n = lib.sbref_subdivide(block, n_items, _ptr(out), cap)
+    return out[: 2 * n].reshape(n, 2)

@@ -1,0 +1,382 @@
+/*
+ * ORACLE — test infrastructure only.
+ *
+ * A plain-C restatement of stablebear's CPU pairwise-integration path, used by
+ * the tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as
+ * the checker / CPU baseline.  Nothing in the product (stablebear_gb300/)
+ * links, imports or calls this file.
+ *
+ * What it restates (paths relative to the stablebear source tree):
+ *   - iterate_rectangles()      include/sbear/algorithms/functional/iterate_rectangles.hpp:37-104
+ *   - max_time_iterator_prior_to() (the a = 0 start)  iterate_rectangles.hpp:23-35
+ *   - integrate()               include/sbear/algorithms/functional/matrix_integrate.hpp:18-29
+ *                               (naive in-order sum  val += (r - l) * op(f, g))
+ *   - compute_row()             matrix_integrate.hpp:80-90  (j from i+1, or from i for the kernel)
+ *   - CpuCrossIntegrationTask   matrix_integrate.hpp:132-143 (dense row-major cdist)
+ *   - OperationL1Dist / OperationLpDist / OperationL2InnerProduct
+ *                               include/sbear/functional/operations.cuh:19-65
+ *   - DistanceMatrix / SymmetricMatrix storage order
+ *                               include/sbear/distance_matrix.hpp:141-146,
+ *                               include/sbear/symmetric_matrix.hpp:248-260
+ *   - b = numeric_limits<T>::max() as the right end of the last rectangle
+ *                               include/sbear/functional/time_point.hpp:10-14
+ * taskflow's for_each_index over rows (matrix_integrate.hpp:69-75) is replaced
+ * by a pthread pool that hands out rows through an atomic counter.
+ *
+ * A second, "truth" oracle accumulates the same rectangles in double-double
+ * arithmetic (Dekker/Knuth TwoSum and an FMA-based TwoProd) and is used to
+ * state the error of every implementation against near-exact sums.
+ *
+ * Build: see oracle/build_oracle.py (gcc -O2 -ffp-contract=off, so that the
+ * same bits come out on x86-64 and aarch64).
+ *
+ * Point layout everywhere: interleaved (t, v) pairs, PCF i occupies points
+ * [offsets[i], offsets[i+1]) — the reference's SimplePoint CSR
+ * (include/sbear/cuda/offset_data_manager.hpp:42-68).
+ */
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define SBO_OP_L1 0
+#define SBO_OP_LP 1
+#define SBO_OP_L2 2
+
+/* ---------------------------------------------------------------------- */
+/* Naive restatement, one instance per precision.                           */
+/* ---------------------------------------------------------------------- */
+
+#define SBO_DEFINE_NAIVE(T, SUF, ABS, POW, TMAX)                                          \
+  static inline T sbo_op_##SUF(int op, T p, T f, T g)                                     \
+  {                                                                                       \
+    /* operations.cuh:19-65 */                                                            \
+    if (op == SBO_OP_L1) return ABS(f - g);                                               \
+    if (op == SBO_OP_LP) return POW(ABS(f - g), p);                                       \
+    return f * g;                                                                         \
+  }                                                                                       \
+                                                                                          \
+  T sbo_finalize_##SUF(int op, T p, T x)                                                  \
+  {                                                                                       \
+    if (op == SBO_OP_LP) return POW(x, (T)1 / p);                                         \
+    return x;                                                                             \
+  }                                                                                       \
+                                                                                          \
+  /* Index of the last point with t <= a, or 0 (iterate_rectangles.hpp:23-35). */         \
+  static size_t sbo_prior_##SUF(const T* pts, uint64_t n, T a)                            \
+  {                                                                                       \
+    size_t lo = 0, hi = (size_t)n; /* upper_bound: first index with a < t */              \
+    while (lo < hi) {                                                                     \
+      size_t mid = lo + (hi - lo) / 2;                                                    \
+      if (a < pts[2 * mid]) hi = mid; else lo = mid + 1;                                  \
+    }                                                                                     \
+    return lo == 0 ? 0 : lo - 1;                                                          \
+  }                                                                                       \
+                                                                                          \
+  /* integrate() with a = 0, b = max (matrix_integrate.hpp:18-29). */                     \
+  T sbo_integrate_##SUF(const T* f, uint64_t lf, const T* g, uint64_t lg, int op, T p)    \
+  {                                                                                       \
+    const T a = (T)0, b = TMAX;                                                           \
+    size_t fi = sbo_prior_##SUF(f, lf, a);                                                \
+    size_t gi = sbo_prior_##SUF(g, lg, a);                                                \
+    T t = a, tprev = a, fv, gv, val = (T)0;                                               \
+    while (t < b) {                                                                       \
+      tprev = t;                                                                          \
+      fv = f[2 * fi + 1];                                                                 \
+      gv = g[2 * gi + 1];                                                                 \
+      int fn = fi + 1 < lf, gn = gi + 1 < lg;                                             \
+      if (fn && gn) {                                                                     \
+        T delta = f[2 * (fi + 1)] - g[2 * (gi + 1)];                                      \
+        if (delta <= 0) ++fi;                                                             \
+        if (delta >= 0) ++gi;                                                             \
+      } else if (fn) {                                                                    \
+        ++fi;                                                                             \
+      } else if (gn) {                                                                    \
+        ++gi;                                                                             \
+      } else {                                                                            \
+        val += (b - tprev) * sbo_op_##SUF(op, p, fv, gv);                                 \
+        return val;                                                                       \
+      }                                                                                   \
+      T hi_t = f[2 * fi] > g[2 * gi] ? f[2 * fi] : g[2 * gi];                             \
+      t = hi_t < b ? hi_t : b;                                                            \
+      val += (t - tprev) * sbo_op_##SUF(op, p, fv, gv);                                   \
+    }                                                                                     \
+    return val;                                                                           \
+  }                                                                                       \
+                                                                                          \
+  /* Count of rectangles the merge emits (including the final one to b). */               \
+  uint64_t sbo_count_segments_##SUF(const T* f, uint64_t lf, const T* g, uint64_t lg)     \
+  {                                                                                       \
+    size_t fi = 0, gi = 0;                                                                \
+    uint64_t n = 0;                                                                       \
+    for (;;) {                                                                            \
+      int fn = fi + 1 < lf, gn = gi + 1 < lg;                                             \
+      ++n;                                                                                \
+      if (fn && gn) {                                                                     \
+        T delta = f[2 * (fi + 1)] - g[2 * (gi + 1)];                                      \
+        if (delta <= 0) ++fi;                                                             \
+        if (delta >= 0) ++gi;                                                             \
+      } else if (fn) ++fi;                                                                \
+      else if (gn) ++gi;                                                                  \
+      else return n;                                                                      \
+    }                                                                                     \
+  }
+
+SBO_DEFINE_NAIVE(float, f32, fabsf, powf, FLT_MAX)
+SBO_DEFINE_NAIVE(double, f64, fabs, pow, DBL_MAX)
+
+/* ---------------------------------------------------------------------- */
+/* Double-double "truth" accumulation of the same rectangles.              */
+/* ---------------------------------------------------------------------- */
+
+typedef struct { double hi, lo; } sbo_dd;
+
+static inline sbo_dd dd_two_sum(double a, double b)
+{
+  double s = a + b;
+  double bb = s - a;
+  double e = (a - (s - bb)) + (b - bb);
+  sbo_dd r = { s, e };
+  return r;
+}
+
+static inline sbo_dd dd_add(sbo_dd x, sbo_dd y)
+{
+  sbo_dd s = dd_two_sum(x.hi, y.hi);
+  sbo_dd t = dd_two_sum(x.lo, y.lo);
+  s.lo += t.hi;
+  s = dd_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return dd_two_sum(s.hi, s.lo);
+}
+
+static inline sbo_dd dd_from_diff(double a, double b) /* exact a - b */
+{
+  return dd_two_sum(a, -b);
+}
+
+static inline sbo_dd dd_mul(sbo_dd x, sbo_dd y)
+{
+  double p = x.hi * y.hi;
+  double e = fma(x.hi, y.hi, -p);
+  e += x.hi * y.lo + x.lo * y.hi;
+  return dd_two_sum(p, e);
+}
+
+static inline sbo_dd dd_abs(sbo_dd x)
+{
+  if (x.hi < 0 || (x.hi == 0 && x.lo < 0)) { x.hi = -x.hi; x.lo = -x.lo; }
+  return x;
+}
+
+/* op evaluated in double-double; Lp uses pow() on the rounded |f - g|. */
+static inline sbo_dd dd_op(int op, double p, double f, double g)
+{
+  if (op == SBO_OP_L1) return dd_abs(dd_from_diff(f, g));
+  if (op == SBO_OP_LP) {
+    sbo_dd d = dd_abs(dd_from_diff(f, g));
+    double base = d.hi + d.lo;
+    double r = pow(base, p);
+    sbo_dd out = { r, 0.0 };
+    return out;
+  }
+  sbo_dd a = { f, 0.0 }, b = { g, 0.0 };
+  return dd_mul(a, b);
+}
+
+/* Same rectangle walk as the naive restatement, but times/values widened to
+ * double and the sum carried in double-double.  The right end of the last
+ * rectangle is the *input* type's max, as in the reference. */
+#define SBO_DEFINE_DD(T, SUF, TMAX)                                                       \
+  double sbo_integrate_dd_##SUF(const T* f, uint64_t lf, const T* g, uint64_t lg,         \
+                                int op, double p)                                         \
+  {                                                                                       \
+    const double b = (double)TMAX;                                                        \
+    size_t fi = sbo_prior_##SUF(f, lf, (T)0);                                             \
+    size_t gi = sbo_prior_##SUF(g, lg, (T)0);                                             \
+    double t = 0.0, tprev = 0.0, fv, gv;                                                  \
+    sbo_dd acc = { 0.0, 0.0 };                                                            \
+    while (t < b) {                                                                       \
+      tprev = t;                                                                          \
+      fv = (double)f[2 * fi + 1];                                                         \
+      gv = (double)g[2 * gi + 1];                                                         \
+      int fn = fi + 1 < lf, gn = gi + 1 < lg;                                             \
+      double right;                                                                       \
+      int last = 0;                                                                       \
+      if (fn && gn) {                                                                     \
+        T delta = f[2 * (fi + 1)] - g[2 * (gi + 1)];                                      \
+        if (delta <= 0) ++fi;                                                             \
+        if (delta >= 0) ++gi;                                                             \
+      } else if (fn) ++fi;                                                                \
+      else if (gn) ++gi;                                                                  \
+      else last = 1;                                                                      \
+      if (last) right = b;                                                                \
+      else {                                                                              \
+        double hi_t = (double)(f[2 * fi] > g[2 * gi] ? f[2 * fi] : g[2 * gi]);            \
+        right = hi_t < b ? hi_t : b;                                                      \
+      }                                                                                   \
+      sbo_dd w = dd_from_diff(right, tprev);                                              \
+      acc = dd_add(acc, dd_mul(w, dd_op(op, p, fv, gv)));                                 \
+      t = right;                                                                          \
+      if (last) break;                                                                    \
+    }                                                                                     \
+    double s = acc.hi + acc.lo;                                                           \
+    if (op == SBO_OP_LP) return pow(s, 1.0 / p);                                          \
+    return s;                                                                             \
+  }
+
+SBO_DEFINE_DD(float, f32, FLT_MAX)
+SBO_DEFINE_DD(double, f64, DBL_MAX)
+
+/* ---------------------------------------------------------------------- */
+/* Row-parallel drivers (the taskflow for_each_index substitute).          */
+/* ---------------------------------------------------------------------- */
+
+/* mode: 0 = cross (dense rows x cols), 1 = pdist (j < i, DistanceMatrix
+ * order), 2 = kernel (j <= i, SymmetricMatrix order).  kind: 0 naive in the
+ * input precision, 1 double-double truth (output always double). */
+typedef struct {
+  int dtype;             /* 0 = f32, 1 = f64 */
+  int kind;
+  int op;
+  double p;
+  int mode;
+  const void* rpts; const uint64_t* roff; uint64_t nr;
+  const void* cpts; const uint64_t* coff; uint64_t nc;
+  const uint64_t* rows;  /* row list to evaluate (NULL = 0..nr-1) */
+  uint64_t nrows;
+  void* out;
+  int compact;           /* 1: write each evaluated row's results back to back */
+  const uint64_t* compact_base; /* per listed row: first output slot when compact */
+  _Atomic uint64_t next;
+} sbo_job;
+
+static inline uint64_t sbo_cond_index(int mode, uint64_t i, uint64_t j)
+{
+  uint64_t r = i > j ? i : j, c = i > j ? j : i;
+  if (mode == 1) return r * (r - 1) / 2 + c; /* distance_matrix.hpp:141-146 */
+  return r * (r + 1) / 2 + c;                /* symmetric_matrix.hpp:257-259 */
+}
+
+static void sbo_eval_row(sbo_job* job, uint64_t k)
+{
+  uint64_t i = job->rows ? job->rows[k] : k;
+  uint64_t jbeg = 0, jend = job->nc;
+  if (job->mode == 1) jend = i;
+  else if (job->mode == 2) jend = i + 1;
+  for (uint64_t j = jbeg; j < jend; ++j) {
+    uint64_t slot;
+    if (job->compact) slot = job->compact_base[k] + (j - jbeg);
+    else if (job->mode == 0) slot = i * job->nc + j;
+    else slot = sbo_cond_index(job->mode, i, j);
+    if (job->dtype == 0) {
+      const float* fp = (const float*)job->rpts + 2 * job->roff[i];
+      const float* gp = (const float*)job->cpts + 2 * job->coff[j];
+      uint64_t lf = job->roff[i + 1] - job->roff[i], lg = job->coff[j + 1] - job->coff[j];
+      if (job->kind == 0) {
+        float v = sbo_integrate_f32(fp, lf, gp, lg, job->op, (float)job->p);
+        ((float*)job->out)[slot] = sbo_finalize_f32(job->op, (float)job->p, v);
+      } else {
+        ((double*)job->out)[slot] = sbo_integrate_dd_f32(fp, lf, gp, lg, job->op, (double)(float)job->p);
+      }
+    } else {
+      const double* fp = (const double*)job->rpts + 2 * job->roff[i];
+      const double* gp = (const double*)job->cpts + 2 * job->coff[j];
+      uint64_t lf = job->roff[i + 1] - job->roff[i], lg = job->coff[j + 1] - job->coff[j];
+      if (job->kind == 0) {
+        double v = sbo_integrate_f64(fp, lf, gp, lg, job->op, job->p);
+        ((double*)job->out)[slot] = sbo_finalize_f64(job->op, job->p, v);
+      } else {
+        ((double*)job->out)[slot] = sbo_integrate_dd_f64(fp, lf, gp, lg, job->op, job->p);
+      }
+    }
+  }
+}
+
+static void* sbo_worker(void* arg)
+{
+  sbo_job* job = (sbo_job*)arg;
+  for (;;) {
+    uint64_t k = atomic_fetch_add(&job->next, 1);
+    if (k >= job->nrows) break;
+    sbo_eval_row(job, k);
+  }
+  return NULL;
+}
+
+static int sbo_run(sbo_job* job, int nthreads)
+{
+  atomic_store(&job->next, 0);
+  if (nthreads <= 1) { sbo_worker(job); return 0; }
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+  if (!th) return -1;
+  int started = 0;
+  for (int t = 0; t < nthreads; ++t) {
+    if (pthread_create(&th[t], NULL, sbo_worker, job) != 0) break;
+    ++started;
+  }
+  if (started == 0) sbo_worker(job);
+  for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+  free(th);
+  return 0;
+}
+
+/* Full pairwise / cross evaluation.  out: naive -> input type, truth -> double. */
+int sbo_evaluate(int dtype, int kind, int op, double p, int mode,
+                 const void* rpts, const uint64_t* roff, uint64_t nr,
+                 const void* cpts, const uint64_t* coff, uint64_t nc,
+                 void* out, int nthreads)
+{
+  sbo_job job;
+  memset(&job, 0, sizeof(job));
+  job.dtype = dtype; job.kind = kind; job.op = op; job.p = p; job.mode = mode;
+  job.rpts = rpts; job.roff = roff; job.nr = nr;
+  if (mode != 0) { cpts = rpts; coff = roff; nc = nr; }
+  job.cpts = cpts; job.coff = coff; job.nc = nc;
+  job.rows = NULL; job.nrows = nr; job.out = out;
+  return sbo_run(&job, nthreads);
+}
+
+/* Evaluate only the listed rows; results of row k are written back to back
+ * starting at compact_base[k] (used for bounded CPU-baseline samples and for
+ * sampled parity checks at full size). */
+int sbo_evaluate_rows(int dtype, int kind, int op, double p, int mode,
+                      const void* rpts, const uint64_t* roff, uint64_t nr,
+                      const void* cpts, const uint64_t* coff, uint64_t nc,
+                      const uint64_t* rows, uint64_t nrows, const uint64_t* compact_base,
+                      void* out, int nthreads)
+{
+  sbo_job job;
+  memset(&job, 0, sizeof(job));
+  job.dtype = dtype; job.kind = kind; job.op = op; job.p = p; job.mode = mode;
+  job.rpts = rpts; job.roff = roff; job.nr = nr;
+  if (mode != 0) { cpts = rpts; coff = roff; nc = nr; }
+  job.cpts = cpts; job.coff = coff; job.nc = nc;
+  job.rows = rows; job.nrows = nrows; job.out = out;
+  job.compact = 1; job.compact_base = compact_base;
+  return sbo_run(&job, nthreads);
+}
+
+/* Total merged rectangles (segments) of a pairwise/cross problem, the work
+ * unit of the throughput metric.  Counted, not estimated. */
+uint64_t sbo_count_total_segments(int dtype, int mode,
+                                  const void* rpts, const uint64_t* roff, uint64_t nr,
+                                  const void* cpts, const uint64_t* coff, uint64_t nc)
+{
+  if (mode != 0) { cpts = rpts; coff = roff; nc = nr; }
+  uint64_t total = 0;
+  for (uint64_t i = 0; i < nr; ++i) {
+    uint64_t jend = mode == 0 ? nc : (mode == 1 ? i : i + 1);
+    for (uint64_t j = 0; j < jend; ++j) {
+      uint64_t lf = roff[i + 1] - roff[i], lg = coff[j + 1] - coff[j];
+      if (dtype == 0)
+        total += sbo_count_segments_f32((const float*)rpts + 2 * roff[i], lf, (const float*)cpts + 2 * coff[j], lg);
+      else
+        total += sbo_count_segments_f64((const double*)rpts + 2 * roff[i], lf, (const double*)cpts + 2 * coff[j], lg);
+    }
+  }
+  return total;
+}

@@ -1,0 +1,431 @@
+// C ABI (include/sbgpu.h) over the engine.  Exceptions stop here and become
+// status codes plus a per-thread message.
+#include "../../include/sbgpu.h"
+#include "sbg_internal.hpp"
+
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <memory>
+#include <mutex>
+#include <thread>
+
+using namespace sbg;
+
+namespace
+{
+  template <typename F>
+  int guarded(F&& f)
+  {
+    try
+    {
+      f();
+      set_last_error("");
+      return SBG_OK;
+    }
+    catch (const Error& e)
+    {
+      set_last_error(e.what());
+      return e.status;
+    }
+    catch (const std::bad_alloc&)
+    {
+      set_last_error("host allocation failed");
+      return SBG_ERR_OUT_OF_MEMORY;
+    }
+    catch (const std::exception& e)
+    {
+      set_last_error(e.what());
+      return SBG_ERR_INTERNAL;
+    }
+    catch (...)
+    {
+      set_last_error("unknown error");
+      return SBG_ERR_INTERNAL;
+    }
+  }
+
+  void check_common(int dtype, int op, double p, int mode)
+  {
+    if (dtype != SBG_F32 && dtype != SBG_F64) throw Error(ST_INVALID_ARGUMENT, "dtype must be SBG_F32 or SBG_F64");
+    if (op != SBG_OP_L1 && op != SBG_OP_LP && op != SBG_OP_L2_INNER) throw Error(ST_INVALID_ARGUMENT, "unknown op");
+    if (op == SBG_OP_LP && !(p >= 1.0)) throw Error(ST_INVALID_ARGUMENT, "p must be >= 1.");
+    if (mode != SBG_SKIP_NONE && mode != SBG_SKIP_LOWER_NODIAG && mode != SBG_SKIP_LOWER)
+      throw Error(ST_INVALID_ARGUMENT, "unknown skip mode");
+  }
+
+  int current_device()
+  {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+    {
+      cudaGetLastError();
+      throw Error(ST_NO_DEVICE, std::string("no CUDA device available: ") + cudaGetErrorString(e));
+    }
+    int d = 0;
+    SBG_CUDA(cudaGetDevice(&d));
+    return d;
+  }
+
+  template <typename T>
+  void run_host(int op, double p, int mode, const void* rp, const uint64_t* ro, uint64_t nr, const void* cp,
+                const uint64_t* co, uint64_t nc, void* out, bool validate, const RunControl& ctl)
+  {
+    PcfSet<T> rows{static_cast<const T*>(rp), ro, nr};
+    PcfSet<T> cols{static_cast<const T*>(cp), co, nc};
+    compute_host<T>(mode, op, p, rows, mode == MODE_CROSS ? &cols : nullptr, static_cast<T*>(out), validate, ctl);
+  }
+}
+
+// ---- the task object (StoppableTask, include/sbear/task.hpp:15-172) ----------
+
+struct sbg_task
+{
+  int dtype = 0, op = 0, mode = 0;
+  double p = 1.0;
+  int device = 0;
+  std::vector<unsigned char> rpts, cpts;
+  std::vector<uint64_t> roff, coff;
+  uint64_t nr = 0, nc = 0;
+  void* out = nullptr;
+
+  std::thread worker;
+  std::atomic<bool> stop{false};
+  std::atomic<bool> finished{false};
+  std::atomic<bool> running{false};
+  std::atomic<uint64_t> total{0}, completed{0}, step{0};
+  mutable std::mutex mu;
+  std::condition_variable cv;
+  std::string desc, unit;
+  int status = SBG_OK;
+  std::string message;
+  bool reported = false;
+
+  void run()
+  {
+    int st = guarded([&] {
+      SBG_CUDA(cudaSetDevice(device));
+      RunControl ctl;
+      ctl.stop = &stop;
+      ctl.progress = [this](uint64_t k) { completed.fetch_add(k); };
+      const void* cp = mode == MODE_CROSS ? (const void*)cpts.data() : nullptr;
+      const uint64_t* co = mode == MODE_CROSS ? coff.data() : nullptr;
+      if (dtype == SBG_F32)
+        run_host<float>(op, p, mode, rpts.data(), roff.data(), nr, cp, co, nc, out, false, ctl);
+      else
+        run_host<double>(op, p, mode, rpts.data(), roff.data(), nr, cp, co, nc, out, false, ctl);
+    });
+    {
+      std::lock_guard<std::mutex> lock(mu);
+      status = st;
+      message = st == SBG_OK ? "" : last_error();
+      finished.store(true);
+    }
+    cv.notify_all();
+  }
+
+  int consume()
+  {
+    if (worker.joinable()) worker.join();
+    std::lock_guard<std::mutex> lock(mu);
+    if (reported) return SBG_OK;
+    reported = true;
+    if (status != SBG_OK) set_last_error(message);
+    return status;
+  }
+};
+
+namespace
+{
+  template <typename T>
+  void copy_set(std::vector<unsigned char>& pts, std::vector<uint64_t>& off, const void* p, const uint64_t* o, uint64_t n)
+  {
+    off.assign(o, o + n + 1);
+    const uint64_t npts = n ? o[n] : 0;
+    pts.resize(std::max<uint64_t>(1, npts) * 2 * sizeof(T));
+    if (npts) std::memcpy(pts.data(), p, npts * 2 * sizeof(T));
+  }
+
+  template <typename T>
+  void validate_set(const void* p, const uint64_t* o, uint64_t n, const char* what)
+  {
+    PcfSet<T> s{static_cast<const T*>(p), o, n};
+    validate_pcfs(s, what);
+  }
+
+  void check_set(const void* p, const uint64_t* o, uint64_t n)
+  {
+    if (n > 0 && (!p || !o)) throw Error(ST_INVALID_ARGUMENT, "null points/offsets");
+    if (n > 0xffffffffull) throw Error(ST_INVALID_ARGUMENT, "too many PCFs");
+  }
+}
+
+extern "C"
+{
+  int sbg_api_version(void) { return SBG_API_VERSION; }
+  const char* sbg_last_error(void) { return last_error(); }
+  const char* sbg_build_type(void) { return "CUDA"; }
+
+  int sbg_get_ngpus(int* n)
+  {
+    return guarded([&] {
+      if (!n) throw Error(ST_INVALID_ARGUMENT, "null n");
+      int c = 0;
+      cudaError_t e = cudaGetDeviceCount(&c);
+      if (e != cudaSuccess) { cudaGetLastError(); c = 0; }
+      int lim = settings().gpuLimit.load();
+      *n = (lim >= 0 && lim < c) ? lim : c;
+    });
+  }
+
+  int sbg_set_force_cpu(int on) { settings().forceCpu.store(on != 0); return SBG_OK; }
+  int sbg_get_force_cpu(void) { return settings().forceCpu.load() ? 1 : 0; }
+  int sbg_set_cuda_threshold(uint64_t n) { settings().cudaThreshold.store(n); return SBG_OK; }
+  uint64_t sbg_get_cuda_threshold(void) { return settings().cudaThreshold.load(); }
+  int sbg_set_block_dim(unsigned x, unsigned y)
+  {
+    if (x == 0 || y == 0) { set_last_error("block dimensions must be positive"); return SBG_ERR_INVALID_ARGUMENT; }
+    settings().blockDimX.store(x);
+    settings().blockDimY.store(y);
+    return SBG_OK;
+  }
+  int sbg_set_min_block_side(uint64_t n) { settings().minBlockSide.store(n); return SBG_OK; }
+  int sbg_limit_gpus(int n) { settings().gpuLimit.store(n); return SBG_OK; }
+  int sbg_limit_cpus(int n) { settings().cpuLimit.store(n); return SBG_OK; }
+  int sbg_set_device_verbose(int on) { settings().deviceVerbose.store(on != 0); return SBG_OK; }
+  int sbg_get_device_verbose(void) { return settings().deviceVerbose.load() ? 1 : 0; }
+
+  int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes)
+  {
+    return guarded([&] {
+      if (warps < 0 || warps > 32) throw Error(ST_INVALID_ARGUMENT, "warps must be in [0, 32]");
+      if (row_chunk < 0 || row_chunk > 1024) throw Error(ST_INVALID_ARGUMENT, "row_chunk must be in [0, 1024]");
+      if (variant < 0 || variant > 2) throw Error(ST_INVALID_ARGUMENT, "variant must be 0, 1 or 2");
+      if (order < 0 || order > 2) throw Error(ST_INVALID_ARGUMENT, "order must be 0, 1 or 2");
+      settings().warps.store(warps);
+      settings().rowChunk.store(row_chunk);
+      settings().variant.store(variant);
+      settings().order.store(order);
+      settings().bandBytes.store(band_bytes);
+    });
+  }
+
+  uint64_t sbg_enumerate_items(int skip_mode, uint64_t n_rows, uint64_t n_cols, uint64_t row_begin,
+                               uint64_t row_end, uint32_t q, uint64_t* out, uint64_t cap)
+  {
+    if (q == 0) return 0;
+    ProblemDesc<float> d{};
+    d.mode = skip_mode;
+    d.nr = n_rows;
+    d.nc = skip_mode == SBG_SKIP_NONE ? n_cols : n_rows;
+    d.row_begin = row_begin;
+    d.row_end = row_end > n_rows ? n_rows : row_end;
+    d.q = q;
+    const uint64_t n = problem_item_count(d);
+    const uint64_t G = ceil_div_u64(d.nc, 32);
+    for (uint64_t id = 0; id < n && id < cap && out; ++id)
+    {
+      uint64_t c, g;
+      if (skip_mode == SBG_SKIP_NONE) { c = id / G; g = id % G; }
+      else tri_decode(id, d.row_begin, d.row_end, q, G, &c, &g);
+      out[2 * id] = c;
+      out[2 * id + 1] = g;
+    }
+    return n;
+  }
+
+  uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols)
+  {
+    return output_count(skip_mode, n_rows, n_cols);
+  }
+
+  int sbg_create_integrate_task(int dtype, int op, double p, int skip_mode, const void* points,
+                                const uint64_t* offsets, uint64_t n, void* out, sbg_task** task)
+  {
+    return guarded([&] {
+      if (!task) throw Error(ST_INVALID_ARGUMENT, "null task pointer");
+      *task = nullptr;
+      check_common(dtype, op, p, skip_mode);
+      if (skip_mode == SBG_SKIP_NONE) throw Error(ST_INVALID_ARGUMENT, "use sbg_create_cdist_task for cdist");
+      check_set(points, offsets, n);
+      if (output_count(skip_mode, n, n) > 0 && !out) throw Error(ST_INVALID_ARGUMENT, "null output");
+      if (dtype == SBG_F32) validate_set<float>(points, offsets, n, "input");
+      else validate_set<double>(points, offsets, n, "input");
+      std::unique_ptr<sbg_task> t(new sbg_task);
+      t->dtype = dtype; t->op = op; t->p = p; t->mode = skip_mode; t->nr = n; t->nc = n; t->out = out;
+      t->device = current_device();
+      if (dtype == SBG_F32) copy_set<float>(t->rpts, t->roff, points, offsets, n);
+      else copy_set<double>(t->rpts, t->roff, points, offsets, n);
+      *task = t.release();
+    });
+  }
+
+  int sbg_create_cdist_task(int dtype, int op, double p, const void* row_points, const uint64_t* row_offsets,
+                            uint64_t n_rows, const void* col_points, const uint64_t* col_offsets, uint64_t n_cols,
+                            void* out, sbg_task** task)
+  {
+    return guarded([&] {
+      if (!task) throw Error(ST_INVALID_ARGUMENT, "null task pointer");
+      *task = nullptr;
+      check_common(dtype, op, p, SBG_SKIP_NONE);
+      check_set(row_points, row_offsets, n_rows);
+      check_set(col_points, col_offsets, n_cols);
+      if (n_rows * n_cols > 0 && !out) throw Error(ST_INVALID_ARGUMENT, "null output");
+      if (dtype == SBG_F32)
+      {
+        validate_set<float>(row_points, row_offsets, n_rows, "X");
+        validate_set<float>(col_points, col_offsets, n_cols, "Y");
+      }
+      else
+      {
+        validate_set<double>(row_points, row_offsets, n_rows, "X");
+        validate_set<double>(col_points, col_offsets, n_cols, "Y");
+      }
+      std::unique_ptr<sbg_task> t(new sbg_task);
+      t->dtype = dtype; t->op = op; t->p = p; t->mode = SBG_SKIP_NONE; t->nr = n_rows; t->nc = n_cols; t->out = out;
+      t->device = current_device();
+      if (dtype == SBG_F32)
+      {
+        copy_set<float>(t->rpts, t->roff, row_points, row_offsets, n_rows);
+        copy_set<float>(t->cpts, t->coff, col_points, col_offsets, n_cols);
+      }
+      else
+      {
+        copy_set<double>(t->rpts, t->roff, row_points, row_offsets, n_rows);
+        copy_set<double>(t->cpts, t->coff, col_points, col_offsets, n_cols);
+      }
+      *task = t.release();
+    });
+  }
+
+  int sbg_task_start(sbg_task* t)
+  {
+    return guarded([&] {
+      if (!t) throw Error(ST_INVALID_ARGUMENT, "null task");
+      if (t->running.exchange(true)) throw Error(ST_INVALID_ARGUMENT, "task already started");
+      t->stop.store(false);
+      t->completed.store(0);
+      {
+        std::lock_guard<std::mutex> lock(t->mu);
+        t->step.fetch_add(1);
+        t->total.store(output_count(t->mode, t->nr, t->nc));
+        t->desc = t->mode == MODE_CROSS ? "Computing cross-distances" : "Computing lower triangle";
+        t->unit = "integral";
+      }
+      t->worker = std::thread([t] { t->run(); });
+    });
+  }
+
+  int sbg_task_wait_for(sbg_task* t, int64_t timeout_ms, int* finished)
+  {
+    if (!t || !finished) { set_last_error("null argument"); return SBG_ERR_INVALID_ARGUMENT; }
+    if (!t->running.load()) { *finished = 1; return SBG_OK; }
+    {
+      std::unique_lock<std::mutex> lock(t->mu);
+      if (!t->cv.wait_for(lock, std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms),
+                          [t] { return t->finished.load(); }))
+      {
+        *finished = 0;
+        return SBG_OK;
+      }
+    }
+    *finished = 1;
+    return t->consume();
+  }
+
+  int sbg_task_wait(sbg_task* t)
+  {
+    if (!t) { set_last_error("null task"); return SBG_ERR_INVALID_ARGUMENT; }
+    if (!t->running.load()) return SBG_OK;
+    {
+      std::unique_lock<std::mutex> lock(t->mu);
+      t->cv.wait(lock, [t] { return t->finished.load(); });
+    }
+    return t->consume();
+  }
+
+  int sbg_task_request_stop(sbg_task* t)
+  {
+    if (!t) { set_last_error("null task"); return SBG_ERR_INVALID_ARGUMENT; }
+    t->stop.store(true);
+    return SBG_OK;
+  }
+
+  int sbg_task_stop_requested(const sbg_task* t) { return (t && t->stop.load()) ? 1 : 0; }
+
+  int sbg_task_progress(const sbg_task* t, uint64_t* total, uint64_t* completed, uint64_t* step)
+  {
+    if (!t) { set_last_error("null task"); return SBG_ERR_INVALID_ARGUMENT; }
+    if (total) *total = t->total.load();
+    if (completed) *completed = t->completed.load();
+    if (step) *step = t->step.load();
+    return SBG_OK;
+  }
+
+  int sbg_task_step_text(const sbg_task* t, char* desc, size_t desc_cap, char* unit, size_t unit_cap)
+  {
+    if (!t) { set_last_error("null task"); return SBG_ERR_INVALID_ARGUMENT; }
+    std::lock_guard<std::mutex> lock(t->mu);
+    if (desc && desc_cap) std::snprintf(desc, desc_cap, "%s", t->desc.c_str());
+    if (unit && unit_cap) std::snprintf(unit, unit_cap, "%s", t->unit.c_str());
+    return SBG_OK;
+  }
+
+  void sbg_task_destroy(sbg_task* t)
+  {
+    if (!t) return;
+    if (t->worker.joinable()) t->worker.join();
+    delete t;
+  }
+
+  int sbg_pairwise_host(int dtype, int op, double p, int skip_mode, const void* row_points,
+                        const uint64_t* row_offsets, uint64_t n_rows, const void* col_points,
+                        const uint64_t* col_offsets, uint64_t n_cols, void* out, int validate)
+  {
+    return guarded([&] {
+      check_common(dtype, op, p, skip_mode);
+      check_set(row_points, row_offsets, n_rows);
+      if (skip_mode == SBG_SKIP_NONE) check_set(col_points, col_offsets, n_cols);
+      (void)current_device();
+      RunControl ctl;
+      if (dtype == SBG_F32)
+        run_host<float>(op, p, skip_mode, row_points, row_offsets, n_rows, col_points, col_offsets, n_cols, out,
+                        validate != 0, ctl);
+      else
+        run_host<double>(op, p, skip_mode, row_points, row_offsets, n_rows, col_points, col_offsets, n_cols, out,
+                         validate != 0, ctl);
+    });
+  }
+
+  int sbg_pairwise_device(int dtype, int op, double p, int skip_mode, const void* row_points,
+                          const uint64_t* row_offsets, uint64_t n_rows, const void* col_points,
+                          const uint64_t* col_offsets, uint64_t n_cols, const uint32_t* row_perm,
+                          const uint32_t* col_perm, uint32_t max_points, void* out, uint64_t out_base,
+                          uint64_t row_begin, uint64_t row_end, void* stream)
+  {
+    return guarded([&] {
+      check_common(dtype, op, p, skip_mode);
+      check_set(row_points, row_offsets, n_rows);
+      if (skip_mode == SBG_SKIP_NONE) check_set(col_points, col_offsets, n_cols);
+      if (output_count(skip_mode, n_rows, n_cols) > 0 && !out) throw Error(ST_INVALID_ARGUMENT, "null output");
+      (void)current_device();
+      if (row_end == 0 || row_end > n_rows) row_end = n_rows;
+      cudaStream_t st = static_cast<cudaStream_t>(stream);
+      if (dtype == SBG_F32)
+      {
+        PcfSet<float> r{static_cast<const float*>(row_points), row_offsets, n_rows};
+        PcfSet<float> c{static_cast<const float*>(col_points), col_offsets, n_cols};
+        compute_device<float>(skip_mode, op, p, r, skip_mode == SBG_SKIP_NONE ? &c : nullptr, row_perm, col_perm,
+                              max_points, static_cast<float*>(out), out_base, row_begin, row_end, st);
+      }
+      else
+      {
+        PcfSet<double> r{static_cast<const double*>(row_points), row_offsets, n_rows};
+        PcfSet<double> c{static_cast<const double*>(col_points), col_offsets, n_cols};
+        compute_device<double>(skip_mode, op, p, r, skip_mode == SBG_SKIP_NONE ? &c : nullptr, row_perm, col_perm,
+                               max_points, static_cast<double*>(out), out_base, row_begin, row_end, st);
+      }
+    });
+  }
+}

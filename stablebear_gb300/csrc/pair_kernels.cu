@@ -1,0 +1,315 @@
+// Pairwise PCF integration kernels (sm_103a).  Design notes are in
+// pair_kernels.cuh; this file holds the device code and its launchers.
+#include "pair_kernels.cuh"
+#include "sbg_internal.hpp"
+
+#include <climits>
+
+namespace sbg
+{
+  namespace
+  {
+    constexpr unsigned FULL = 0xffffffffu;
+
+    __device__ __forceinline__ uint32_t warp_max_u32(uint32_t x)
+    {
+      return __reduce_max_sync(FULL, x);
+    }
+    __device__ __forceinline__ uint32_t warp_min_u32(uint32_t x)
+    {
+      return __reduce_min_sync(FULL, x);
+    }
+
+    // Clamp a breakpoint time into [.., TMAX]; NaN and +inf become TMAX.  This
+    // keeps every time the merge compares <= TMAX, so a column can never be
+    // advanced past its sentinel, whatever the input holds.
+    template <typename T>
+    __device__ __forceinline__ T clamp_time(T t) { return fmin(t, tmax_of<T>()); }
+
+    template <typename T>
+    __device__ __forceinline__ int find_problem(const ProblemDesc<T>* probs, int n, uint64_t item)
+    {
+      int lo = 0, hi = n - 1;
+      while (lo < hi)
+      {
+        int mid = (lo + hi + 1) >> 1;
+        if (probs[mid].item_begin <= item) lo = mid; else hi = mid - 1;
+      }
+      return lo;
+    }
+
+    // Kahan step adding a block sum; a non-finite running sum (the last
+    // rectangle of a pair whose tails are non-zero runs to TMAX) keeps a zero
+    // compensation so it cannot turn into NaN.
+    template <typename T>
+    __device__ __forceinline__ void kahan_add(T& acc, T& comp, T x)
+    {
+      const T y = x - comp;
+      const T s = acc + y;
+      comp = isfinite(s) ? (s - acc) - y : T(0);
+      acc = s;
+    }
+  }
+
+  // The merge of one row (warp-shared, segment layout at pf) against one
+  // column per lane (segment layout at pg, stride GS elements between
+  // consecutive elements of the same column).  `steps` is warp-uniform.
+  // FCLAMP: the row pointer stops at its last element (global-memory variant,
+  // no padding); otherwise the row buffer is padded with sentinel copies.
+  template <typename T, int K, int U, int GS, bool FCLAMP>
+  __device__ __forceinline__ T merge_pair(const Elem<T>* __restrict__ pf, const Elem<T>* __restrict__ pg,
+                                          uint32_t steps, uint32_t rlen, T p)
+  {
+    Elem<T> F = pf[0];
+    Elem<T> G = pg[0];
+    uint32_t fi = 0;
+    T t = T(0), acc = T(0), comp = T(0);
+    const uint32_t nblk = (steps + U - 1) / U;
+    for (uint32_t b = 0; b < nblk; ++b)
+    {
+      T blk = T(0);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+      {
+        const bool takeF = F.tn <= G.tn;
+        const T tn = takeF ? F.tn : G.tn;
+        blk += PairOp<K>::seg(tn - t, F.v, G.v, p);
+        t = tn;
+        if (FCLAMP)
+        {
+          fi = min(fi + (takeF ? 1u : 0u), rlen - 1);
+          pg += takeF ? 0 : GS;
+          F = pf[fi];
+        }
+        else
+        {
+          pf += takeF ? 1 : 0;
+          pg += takeF ? 0 : GS;
+          F = *pf;
+        }
+        G = *pg;
+      }
+      kahan_add(acc, comp, blk);
+    }
+    return PairOp<K>::fin(acc - comp, p);
+  }
+
+  // Persistent kernel.  SMEM = true stages the item's 32 columns and each
+  // warp's row in shared memory; SMEM = false reads the packed segment layout
+  // (pack_segments_kernel) from global memory through L1.
+  template <typename T, int K, int U, bool SMEM>
+  __global__ void __launch_bounds__(1024, 1) pairs_kernel(const __grid_constant__ LaunchParams<T> L)
+  {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Elem<T>* cols = reinterpret_cast<Elem<T>*>(smem_raw);
+    Elem<T>* rows = cols + (size_t)L.lmax_c * 32;
+    __shared__ unsigned long long s_item;
+    __shared__ unsigned int s_next_row;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    Elem<T>* rbuf = rows + (size_t)warp * L.row_cap;
+    const T TM = tmax_of<T>();
+
+    for (;;)
+    {
+      if (threadIdx.x == 0)
+      {
+        s_item = atomicAdd(L.queue, 1ull);
+        s_next_row = 0;
+      }
+      __syncthreads();
+      const unsigned long long item = s_item;
+      if (item >= L.total_items) break;
+
+      const ProblemDesc<T>* Pp = L.probs ? L.probs + find_problem(L.probs, L.n_probs, item) : &L.one;
+      const int mode = Pp->mode;
+      const uint64_t nc = Pp->nc;
+      const uint64_t G = ceil_div_u64(nc, 32);
+      const uint64_t local = item - Pp->item_begin;
+      uint64_t c, g;
+      if (mode == MODE_CROSS) { c = local / G; g = local % G; }
+      else tri_decode(local, Pp->row_begin, Pp->row_end, Pp->q, G, &c, &g);
+      uint64_t row_lo = Pp->row_begin + c * 32ull * Pp->q;
+      uint64_t row_hi = row_lo + 32ull * Pp->q;
+      if (row_hi > Pp->row_end) row_hi = Pp->row_end;
+      const uint64_t col0 = 32ull * g;
+      if (mode != MODE_CROSS)
+      {
+        const uint64_t first = col0 + (mode == MODE_PDIST ? 1 : 0);
+        if (row_lo < first) row_lo = first;
+      }
+
+      // This lane's column.  Lanes past the last column mirror lane 0's
+      // column (their results are discarded) so the warp-uniform step count
+      // and the row padding stay valid for them.
+      const uint64_t cj = col0 + lane;
+      const bool cvalid = cj < nc;
+      const uint64_t cj_eff = cvalid ? cj : col0;
+      const uint64_t corig = Pp->cperm ? Pp->cperm[cj_eff] : cj_eff;
+      const uint64_t coff = Pp->coff[corig];
+      const uint32_t clen = (uint32_t)(Pp->coff[corig + 1] - coff);
+      const uint32_t maxlc = warp_max_u32(clen);
+      const T p = Pp->p;
+
+      bool item_ok = true;
+      if (SMEM)
+      {
+        if (maxlc > L.lmax_c || __any_sync(FULL, clen == 0)) item_ok = false;  // host sized lmax_c; never expected
+        else
+        {
+          const T* cp = Pp->cpts + 2 * coff;
+          for (uint32_t k = warp; k < maxlc; k += nwarps)
+          {
+            if (k < clen)
+            {
+              const T tk = cp[2 * k], vk = cp[2 * k + 1];
+              cols[(size_t)k * 32 + lane].v = vk;
+              if (k > 0) cols[(size_t)(k - 1) * 32 + lane].tn = clamp_time(tk);
+              if (k + 1 == clen) cols[(size_t)k * 32 + lane].tn = TM;
+            }
+          }
+        }
+        __syncthreads();
+      }
+
+      if (item_ok)
+      {
+        for (;;)
+        {
+          unsigned r = 0;
+          if (lane == 0) r = atomicAdd(&s_next_row, 1u);
+          r = __shfl_sync(FULL, r, 0);
+          const uint64_t i = row_lo + r;
+          if (i >= row_hi) break;
+
+          const uint64_t iorig = Pp->rperm ? Pp->rperm[i] : i;
+          const uint64_t roff = Pp->roff[iorig];
+          const uint32_t rlen = (uint32_t)(Pp->roff[iorig + 1] - roff);
+          const bool ok = cvalid && (mode == MODE_CROSS || (mode == MODE_PDIST ? cj < i : cj <= i));
+          if (!__any_sync(FULL, ok) || rlen == 0) continue;
+          const uint32_t steps = rlen + maxlc - 1;
+
+          T res;
+          if (SMEM)
+          {
+            // Row in segment layout plus sentinel padding: at most
+            // steps + U - 1 advances can reach the row side.
+            const uint32_t pad_end = rlen + maxlc + U;
+            if (pad_end > L.row_cap) continue;  // host sized row_cap; never expected
+            const T* rp = Pp->rpts + 2 * roff;
+            for (uint32_t k = lane; k < rlen; k += 32)
+            {
+              const T tk = rp[2 * k], vk = rp[2 * k + 1];
+              rbuf[k].v = vk;
+              if (k > 0) rbuf[k - 1].tn = clamp_time(tk);
+            }
+            const T vlast = rp[2 * (rlen - 1) + 1];
+            for (uint32_t k = rlen - 1 + lane; k < pad_end; k += 32)
+            {
+              rbuf[k].v = vlast;
+              rbuf[k].tn = TM;
+            }
+            __syncwarp();
+            res = merge_pair<T, K, U, 32, false>(rbuf, cols + lane, steps, rlen, p);
+            __syncwarp();
+          }
+          else
+          {
+            const Elem<T>* pk = reinterpret_cast<const Elem<T>*>(Pp->rpts);  // packed rows
+            const Elem<T>* ck = reinterpret_cast<const Elem<T>*>(Pp->cpts);  // packed columns
+            res = merge_pair<T, K, U, 1, true>(pk + roff, ck + coff, steps, rlen, p);
+          }
+
+          if (ok)
+          {
+            const uint64_t jorig = corig;
+            uint64_t idx;
+            if (mode == MODE_CROSS) idx = iorig * Pp->ld + jorig;
+            else idx = condensed_index(mode, iorig, jorig);
+            const uint64_t rel = idx - Pp->out_base;  // wraps for idx < out_base
+            if (rel < Pp->out_count) Pp->out[rel] = res;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // Segment layout in global memory: element k of PCF i (at the PCF's own
+  // CSR offset) holds (v_k, t_{k+1}), the last one (v_{L-1}, TMAX).
+  template <typename T>
+  __global__ void pack_segments_kernel(const T* __restrict__ pts, const uint64_t* __restrict__ off, uint64_t n,
+                                       Elem<T>* __restrict__ out)
+  {
+    const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+    for (uint64_t i = w; i < n; i += nw)
+    {
+      const uint64_t o = off[i];
+      const uint64_t len = off[i + 1] - o;
+      for (uint64_t k = lane; k < len; k += 32)
+      {
+        Elem<T> e;
+        e.v = pts[2 * (o + k) + 1];
+        e.tn = (k + 1 < len) ? clamp_time(pts[2 * (o + k + 1)]) : tmax_of<T>();
+        out[o + k] = e;
+      }
+    }
+  }
+
+  // ---- launchers ------------------------------------------------------------
+
+  template <typename T, bool SMEM>
+  static cudaError_t launch_op(int opk, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const LaunchParams<T>& L)
+  {
+    constexpr int U = 8;
+    void (*fn)(const LaunchParams<T>) = nullptr;
+    switch (opk)
+    {
+      case OPK_L1: fn = pairs_kernel<T, OPK_L1, U, SMEM>; break;
+      case OPK_L2DIST: fn = pairs_kernel<T, OPK_L2DIST, U, SMEM>; break;
+      case OPK_LP: fn = pairs_kernel<T, OPK_LP, U, SMEM>; break;
+      case OPK_INNER: fn = pairs_kernel<T, OPK_INNER, U, SMEM>; break;
+      default: return cudaErrorInvalidValue;
+    }
+    if (SMEM)
+    {
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    fn<<<grid, block, smem, s>>>(L);
+    return cudaGetLastError();
+  }
+
+  template <typename T>
+  cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, bool smem_variant, int warps, int grid,
+                           size_t smem_bytes, cudaStream_t s)
+  {
+    dim3 g((unsigned)grid), b((unsigned)(warps * 32));
+    if (smem_variant) return launch_op<T, true>(opk, g, b, smem_bytes, s, L);
+    return launch_op<T, false>(opk, g, b, 0, s, L);
+  }
+
+  template <typename T>
+  cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, int sms, cudaStream_t s)
+  {
+    if (n == 0) return cudaSuccess;
+    uint64_t blocks = (n + 7) / 8;
+    uint64_t cap = (uint64_t)sms * 8;
+    if (blocks > cap) blocks = cap;
+    pack_segments_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(pts, off, n, out);
+    return cudaGetLastError();
+  }
+
+  constexpr int kUnroll = 8;
+
+  template cudaError_t launch_pairs<float>(const LaunchParams<float>&, int, bool, int, int, size_t, cudaStream_t);
+  template cudaError_t launch_pairs<double>(const LaunchParams<double>&, int, bool, int, int, size_t, cudaStream_t);
+  template cudaError_t launch_pack<float>(const float*, const uint64_t*, uint64_t, Elem<float>*, int, cudaStream_t);
+  template cudaError_t launch_pack<double>(const double*, const uint64_t*, uint64_t, Elem<double>*, int, cudaStream_t);
+
+  int kernel_unroll() { return kUnroll; }
+}

@@ -1,0 +1,181 @@
+// Internal host-side declarations shared by the engine, the task layer and
+// the C ABI.  Not installed; the public surface is include/sbgpu.h and
+// include/sbgpu/*.hpp.
+#pragma once
+
+#include "pair_kernels.cuh"
+
+#include <atomic>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace sbg
+{
+  // Status codes of the C ABI (include/sbgpu.h).
+  enum Status : int
+  {
+    ST_OK = 0,
+    ST_INVALID_ARGUMENT = -1,
+    ST_INVALID_INPUT = -2,
+    ST_CUDA = -3,
+    ST_OUT_OF_MEMORY = -4,
+    ST_CANCELLED = -5,
+    ST_NO_DEVICE = -6,
+    ST_TIMEOUT = -7,
+    ST_INTERNAL = -8,
+    ST_LOGIC = -9,
+  };
+
+  // Exception carrying a C-ABI status; converted at the ABI boundary.
+  struct Error : std::runtime_error
+  {
+    int status;
+    Error(int st, const std::string& msg) : std::runtime_error(msg), status(st) { }
+  };
+
+  // "file:line: <cuda message>", as the reference's CHK_CUDA does
+  // (include/sbear/cuda/cuda_util.cuh:8-10), raised as an Error.
+  [[noreturn]] void throw_cuda(cudaError_t e, const char* file, int line);
+#define SBG_CUDA(expr)                                      \
+  do {                                                      \
+    cudaError_t sbg_e_ = (expr);                            \
+    if (sbg_e_ != cudaSuccess) ::sbg::throw_cuda(sbg_e_, __FILE__, __LINE__); \
+  } while (0)
+
+  void set_last_error(const std::string& msg);
+  const char* last_error();
+
+  // Process-wide settings; mirrors sb::Settings (include/sbear/settings.hpp:8-23).
+  struct Settings
+  {
+    std::atomic<bool> forceCpu{false};
+    std::atomic<uint64_t> cudaThreshold{500};
+    std::atomic<bool> deviceVerbose{false};
+    std::atomic<unsigned> blockDimX{1};
+    std::atomic<unsigned> blockDimY{32};
+    std::atomic<uint64_t> minBlockSide{0};
+    std::atomic<int> gpuLimit{-1};
+    std::atomic<int> cpuLimit{-1};
+    // Engine knobs (0 = automatic).
+    std::atomic<int> warps{0};
+    std::atomic<int> rowChunk{0};        // Q: rows per work item = 32 * Q
+    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory, 2 global-memory
+    std::atomic<int> order{0};           // 0 auto, 1 caller order, 2 length-sorted
+    std::atomic<uint64_t> bandBytes{0};  // output bytes per pipeline band (0 = auto)
+  };
+  Settings& settings();
+
+  // RAII device buffer.
+  class DeviceBuffer
+  {
+  public:
+    DeviceBuffer() = default;
+    explicit DeviceBuffer(size_t bytes) { reset(bytes); }
+    ~DeviceBuffer() { release(); }
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    DeviceBuffer(DeviceBuffer&& o) noexcept : m_ptr(o.m_ptr), m_bytes(o.m_bytes) { o.m_ptr = nullptr; o.m_bytes = 0; }
+    DeviceBuffer& operator=(DeviceBuffer&& o) noexcept
+    {
+      if (this != &o) { release(); m_ptr = o.m_ptr; m_bytes = o.m_bytes; o.m_ptr = nullptr; o.m_bytes = 0; }
+      return *this;
+    }
+    void reset(size_t bytes);
+    void release();
+    void* get() const { return m_ptr; }
+    template <typename U> U* as() const { return static_cast<U*>(m_ptr); }
+    size_t bytes() const { return m_bytes; }
+
+  private:
+    void* m_ptr = nullptr;
+    size_t m_bytes = 0;
+  };
+
+  struct DeviceInfo
+  {
+    int device = 0;
+    int sms = 0;
+    size_t smem_optin = 0;
+  };
+  DeviceInfo device_info();
+
+  // A set of PCFs in the reference's CSR layout.
+  template <typename T>
+  struct PcfSet
+  {
+    const T* pts = nullptr;        // interleaved (t, v)
+    const uint64_t* off = nullptr; // n + 1 offsets
+    uint64_t n = 0;
+  };
+
+  // Host-side checks of the input contract (pypcf_support.hpp:76-89):
+  // offsets non-decreasing from 0, every PCF non-empty, first time 0, times
+  // non-decreasing and finite.  Throws Error(ST_INVALID_INPUT).
+  template <typename T>
+  void validate_pcfs(const PcfSet<T>& s, const char* what);
+
+  // Launch plan for one pairwise problem on the device.
+  struct Plan
+  {
+    bool smem = true;
+    int warps = 16;
+    int grid = 1;
+    uint32_t q = 1;
+    uint32_t lmax_c = 0;
+    uint32_t row_cap = 0;
+    size_t smem_bytes = 0;
+  };
+
+  // Length statistics used for planning.
+  struct LengthStats
+  {
+    uint32_t lmax = 0;
+    uint32_t lmin = 0;
+    double mean = 0.0;
+  };
+
+  template <typename T>
+  Plan make_plan(int mode, uint64_t n_rows, uint64_t n_cols, const LengthStats& rows, const LengthStats& cols,
+                 const DeviceInfo& dev);
+
+  int op_kind(int op, double p);
+
+  // Kernel launchers (pair_kernels.cu).
+  template <typename T>
+  cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, bool smem_variant, int warps, int grid,
+                           size_t smem_bytes, cudaStream_t s);
+  template <typename T>
+  cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, int sms, cudaStream_t s);
+  int kernel_unroll();
+
+  // Control block of one host-side run (progress, cancellation).
+  struct RunControl
+  {
+    std::atomic<bool>* stop = nullptr;
+    std::function<void(uint64_t)> progress;
+  };
+
+  // Whole pipeline for host buffers: H2D of the CSR, kernel launches over
+  // row bands, D2H of each band straight into the caller's condensed/dense
+  // output.  mode: MODE_PDIST, MODE_KERNEL (cols ignored) or MODE_CROSS.
+  template <typename T>
+  void compute_host(int mode, int op, double p, const PcfSet<T>& rows, const PcfSet<T>* cols, T* out,
+                    bool validate, const RunControl& ctl);
+
+  // Stream-ordered computation on device buffers.  Uses cached scratch for
+  // the descriptor and queue counter; packed copies for the global-memory
+  // variant are allocated per call.
+  template <typename T>
+  void compute_device(int mode, int op, double p, const PcfSet<T>& rows, const PcfSet<T>* cols,
+                      const uint32_t* rperm, const uint32_t* cperm, uint32_t lmax, T* out, uint64_t out_base,
+                      uint64_t row_begin, uint64_t row_end, cudaStream_t stream);
+
+  uint64_t output_count(int mode, uint64_t n_rows, uint64_t n_cols);
+  uint64_t row_output_start(int mode, uint64_t row, uint64_t n_cols);
+}

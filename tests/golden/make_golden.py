@@ -1,0 +1,118 @@
+"""Generate the golden fixtures in this directory from the stablebear
+reference's own code.
+
+Runs only where the reference tree is present: it compiles
+``oracle/ref_harness.cpp`` against the reference's unmodified headers
+(``oracle/build_oracle.py``) and records, for seeded small inputs, the
+reference's outputs in its own DistanceMatrix / SymmetricMatrix / dense
+layouts.  The GPU tests compare the CUDA path against these files, so they
+need neither the reference nor the oracle at run time.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as orc  # noqa: E402
+from stablebear_gb300 import synthetic  # noqa: E402
+
+
+def _ragged(n, lo, hi, dtype, seed):
+    return synthetic.gaussian(n, synthetic.uniform_lengths(lo, hi), dtype, seed)
+
+
+def _with_tails(pts, off, seed):
+    """Give some PCFs non-zero last values (the last rectangle then runs to
+    numeric_limits<T>::max(), as in the reference)."""
+    rng = np.random.default_rng(seed)
+    pts = pts.copy()
+    last = off[1:].astype(np.int64) - 1
+    pick = rng.random(len(last)) < 0.15
+    pts[last[pick], 1] = rng.uniform(-0.5, 0.5, size=pick.sum()).astype(pts.dtype)
+    return pts
+
+
+def _with_ties(pts, off, seed, dtype):
+    """Snap times onto a coarse grid so PCFs share breakpoint times (ties
+    across PCFs) while staying strictly increasing within each PCF."""
+    rng = np.random.default_rng(seed)
+    pts = pts.copy()
+    lens = np.diff(off.astype(np.int64))
+    for i in range(len(lens)):
+        a, b = int(off[i]), int(off[i + 1])
+        steps = rng.integers(1, 3, size=b - a).astype(np.float64)
+        steps[0] = 0.0
+        pts[a:b, 0] = (np.cumsum(steps) * 0.5).astype(dtype)
+    return pts
+
+
+def main():
+    if orc.ref_lib() is None:
+        raise SystemExit("reference tree absent: cannot generate golden fixtures")
+    cases = []
+    for dt, tag in ((np.float32, "f32"), (np.float64, "f64")):
+        pts, off = _ragged(48, 1, 40, dt, seed=11)
+        cases.append((f"ragged_{tag}", pts, off))
+        cases.append((f"tails_{tag}", _with_tails(pts, off, 5), off))
+        cases.append((f"ties_{tag}", _with_ties(pts, off, 7, dt), off))
+        ypts, yoff = _ragged(17, 1, 30, dt, seed=13)
+        cases.append((f"cols_{tag}", ypts, yoff))
+
+    out = {}
+    for name, pts, off in cases:
+        out[f"{name}__points"] = pts
+        out[f"{name}__offsets"] = off
+    for name, pts, off in cases:
+        if name.startswith("cols_"):
+            continue
+        tag = name[-3:]
+        ypts, yoff = out[f"cols_{tag}__points"], out[f"cols_{tag}__offsets"]
+        out[f"{name}__pdist_l1"] = orc.ref_evaluate(pts, off, op=orc.OP_L1, mode=orc.MODE_PDIST)
+        out[f"{name}__pdist_l2"] = orc.ref_evaluate(pts, off, op=orc.OP_LP, p=2.0, mode=orc.MODE_PDIST)
+        out[f"{name}__pdist_l3"] = orc.ref_evaluate(pts, off, op=orc.OP_LP, p=3.0, mode=orc.MODE_PDIST)
+        out[f"{name}__kernel"] = orc.ref_evaluate(pts, off, op=orc.OP_L2, mode=orc.MODE_KERNEL)
+        out[f"{name}__cdist_l1"] = orc.ref_evaluate(pts, off, op=orc.OP_L1, mode=orc.MODE_CROSS,
+                                                    col_points=ypts, col_offsets=yoff)
+        out[f"{name}__cdist_l2k"] = orc.ref_evaluate(pts, off, op=orc.OP_L2, mode=orc.MODE_CROSS,
+                                                     col_points=ypts, col_offsets=yoff)
+        out[f"{name}__cdist_l15"] = orc.ref_evaluate(pts, off, op=orc.OP_LP, p=1.5, mode=orc.MODE_CROSS,
+                                                     col_points=ypts, col_offsets=yoff)
+        # FP64 double-double truth for the same problems
+        out[f"{name}__pdist_l1_truth"] = orc.evaluate(pts, off, op=orc.OP_L1, mode=orc.MODE_PDIST, truth=True)
+        out[f"{name}__kernel_truth"] = orc.evaluate(pts, off, op=orc.OP_L2, mode=orc.MODE_KERNEL, truth=True)
+    path = os.path.join(HERE, "reference_pairwise.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+    # The reference's rectangle walk on its own unit-test PCFs, kept as rows
+    # (left, right, f, g): test/test_iterate_rectangles.cpp:18-19 inputs.
+    f = np.array([[0., 3.], [1., 2.], [4., 5.], [6., 0.]])
+    g = np.array([[0., 2.], [3., 4.], [4., 2.], [5., 1.], [8., 3.]])
+    rects = {
+        "full": orc.ref_rectangles(f, g),
+        "end_early": orc.ref_rectangles(f, g, 0.0, 4.5),
+        "start_late": orc.ref_rectangles(f, g, 2.0),
+    }
+    np.savez(os.path.join(HERE, "reference_rectangles.npz"), f=f, g=g, **rects)
+
+    # CudaBlockScheduler blocks for a few configurations.
+    sched = {}
+    for k, (nr, nc, mo, ns, lower, ms) in enumerate([
+            (10, 10, 16, 1, True, 0), (100, 100, 400, 4, True, 0), (100, 37, 400, 4, False, 0),
+            (1000, 1000, 10000, 32, True, 64), (5, 7, 1, 1, False, 0), (257, 257, 1 << 20, 32, True, 0)]):
+        blocks, mh, mw = orc.ref_schedule(nr, nc, mo, ns, lower, ms)
+        sched[f"cfg{k}"] = np.array([nr, nc, mo, ns, int(lower), ms, mh, mw], dtype=np.uint64)
+        sched[f"blocks{k}"] = blocks
+    np.savez(os.path.join(HERE, "reference_scheduler.npz"), **sched)
+
+
+if __name__ == "__main__":
+    main()

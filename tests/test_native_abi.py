@@ -1,0 +1,150 @@
+"""The C-ABI library: builds, loads, exports every declared symbol, and its
+host-only logic (argument checks, work-item tiling) — no GPU needed."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "sbgpu.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from stablebear_gb300 import build, _native
+    build.build()
+    return _native.lib()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sbg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from stablebear_gb300 import _native
+    names = declared_functions()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(lib, name), f"{name} declared in sbgpu.h but not exported"
+        assert name in _native.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_version_and_build_type(lib):
+    assert lib.sbg_api_version() == 1
+    assert lib.sbg_build_type() == b"CUDA"
+
+
+def test_argument_errors_need_no_device(lib):
+    h = ctypes.c_void_p()
+    pts = np.zeros((2, 2), np.float32)
+    off = np.array([0, 1, 2], np.uint64)
+    out = np.zeros(1, np.float32)
+    P = lambda a: ctypes.c_void_p(a.ctypes.data)
+    # unknown dtype
+    assert lib.sbg_create_integrate_task(7, 0, 1.0, 1, P(pts), P(off), 2, P(out), ctypes.byref(h)) == -1
+    # p < 1 for Lp
+    assert lib.sbg_create_integrate_task(0, 1, 0.5, 1, P(pts), P(off), 2, P(out), ctypes.byref(h)) == -1
+    assert b"p must be >= 1" in lib.sbg_last_error()
+    # cdist through the pairwise factory is rejected
+    assert lib.sbg_create_integrate_task(0, 0, 1.0, 0, P(pts), P(off), 2, P(out), ctypes.byref(h)) == -1
+    assert lib.sbg_set_tuning(99, 0, 0, 0, 0) == -1
+    assert lib.sbg_set_block_dim(0, 1) == -1
+
+
+def test_invalid_pcf_input_rejected_before_device(lib):
+    h = ctypes.c_void_p()
+    P = lambda a: ctypes.c_void_p(a.ctypes.data)
+    out = np.zeros(1, np.float64)
+    off = np.array([0, 2, 3], np.uint64)
+    unsorted = np.array([[0, 1], [-1, 2], [0, 0]], np.float64)
+    assert lib.sbg_create_integrate_task(1, 0, 1.0, 1, P(unsorted), P(off), 2, P(out), ctypes.byref(h)) == -2
+    assert b"non-decreasing" in lib.sbg_last_error()
+    bad_t0 = np.array([[1, 1], [2, 2], [0, 0]], np.float64)
+    assert lib.sbg_create_integrate_task(1, 0, 1.0, 1, P(bad_t0), P(off), 2, P(out), ctypes.byref(h)) == -2
+    assert b"t=0" in lib.sbg_last_error()
+    nan_t = np.array([[0, 1], [np.nan, 2], [0, 0]], np.float64)
+    assert lib.sbg_create_integrate_task(1, 0, 1.0, 1, P(nan_t), P(off), 2, P(out), ctypes.byref(h)) == -2
+    empty = np.array([0, 0, 3], np.uint64)
+    ok = np.array([[0, 1], [1, 2], [2, 0]], np.float64)
+    assert lib.sbg_create_integrate_task(1, 0, 1.0, 1, P(ok), P(empty), 2, P(out), ctypes.byref(h)) == -2
+    assert b"no breakpoints" in lib.sbg_last_error()
+
+
+def test_settings_roundtrip(lib):
+    import stablebear_gb300 as sb
+    sb.set_cuda_threshold(123)
+    assert sb.get_cuda_threshold() == 123
+    sb.set_cuda_threshold(500)
+    sb.set_device_verbose(True)
+    assert lib.sbg_get_device_verbose() == 1
+    sb.set_device_verbose(False)
+    sb.force_cpu(True)
+    assert lib.sbg_get_force_cpu() == 1
+    sb.force_cpu(False)
+    sb.set_tuning()
+
+
+def _items(lib, mode, nr, nc, rb, re, q):
+    n = lib.sbg_enumerate_items(mode, nr, nc, rb, re, q, None, 0)
+    buf = np.zeros(2 * max(n, 1), np.uint64)
+    lib.sbg_enumerate_items(mode, nr, nc, rb, re, q, ctypes.c_void_p(buf.ctypes.data), n)
+    return buf[: 2 * n].reshape(-1, 2)
+
+
+def _covered(items, mode, nr, nc, rb, re, q):
+    """Expand items to the set of (i, j) pairs the kernel visits (same row /
+    lane masks as pairs_kernel), with multiplicity."""
+    seen = np.zeros((nr, nc), np.int64)
+    for c, g in items:
+        lo = rb + int(c) * 32 * q
+        hi = min(lo + 32 * q, re)
+        col0 = 32 * int(g)
+        if mode != 0:
+            lo = max(lo, col0 + (1 if mode == 1 else 0))
+        for i in range(lo, hi):
+            for j in range(col0, min(col0 + 32, nc)):
+                if mode == 0 or (j < i if mode == 1 else j <= i):
+                    seen[i, j] += 1
+    return seen
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("n,q", [(1, 1), (2, 1), (31, 1), (32, 1), (33, 1), (100, 2), (200, 1), (257, 4), (300, 16)])
+def test_work_items_tile_exactly_once(lib, mode, n, q):
+    nc = n if mode else max(1, n // 2 + 3)
+    items = _items(lib, mode, n, nc, 0, n, q)
+    seen = _covered(items, mode, n, nc, 0, n, q)
+    want = np.ones((n, nc), np.int64)
+    if mode == 1:
+        want = np.tril(want, -1)
+    elif mode == 2:
+        want = np.tril(want)
+    np.testing.assert_array_equal(seen, want)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_work_items_of_bands_tile_exactly_once(lib, mode):
+    n, q = 700, 2
+    nc = n if mode else 90
+    seen = np.zeros((n, nc), np.int64)
+    bands = [(0, 64), (64, 320), (320, 448), (448, 700)]
+    for rb, re in bands:
+        seen += _covered(_items(lib, mode, n, nc, rb, re, q), mode, n, nc, rb, re, q)
+    want = np.ones((n, nc), np.int64)
+    if mode == 1:
+        want = np.tril(want, -1)
+    elif mode == 2:
+        want = np.tril(want)
+    np.testing.assert_array_equal(seen, want)
+
+
+def test_output_count(lib):
+    assert lib.sbg_output_count(1, 5, 5) == 10
+    assert lib.sbg_output_count(2, 5, 5) == 15
+    assert lib.sbg_output_count(0, 5, 7) == 35
+    assert lib.sbg_output_count(1, 0, 0) == 0
