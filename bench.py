@@ -247,7 +247,7 @@ def main():
     rows = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        target = args.cpu_sample_rows * n / 2 if args.cpu_sample_rows else 6.0e6 * threads / 16
+        target = args.cpu_sample_rows * n / 2 if args.cpu_sample_rows else 5.0e7 * threads / 16
         rows = sample_rows(n, target)
         rate, dt, npairs, vals, starts = cpu_baseline(pts, off, rows, threads)
         host = out.cpu().numpy() if pairs <= 6_000_000_000 else None

@@ -90,7 +90,8 @@ int sbg_limit_cpus(int n);
 int sbg_set_device_verbose(int on);
 int sbg_get_device_verbose(void);
 /* Engine knobs (0 = automatic): warps per CTA, rows per work item / 32,
- * variant (1 shared-memory, 2 global-memory), order (1 caller's, 2 sorted
+ * variant (1 shared-memory, 2 global-memory, 3 shared-memory with a pointer
+ * walk instead of index arithmetic), order (1 caller's, 2 sorted
  * by breakpoint count), output bytes per pipeline band. */
 int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes);
 

@@ -173,6 +173,7 @@ namespace sbg
     int warps = 0;
     if (variant != 2)
     {
+      // (variants 1 and 3 both stage in shared memory)
       const int cands[] = {32, 24, 16, 12, 8, 4};
       for (int w : cands)
       {
@@ -180,11 +181,12 @@ namespace sbg
         if (smem_for(w) + reserve <= dev.smem_optin) { warps = w; break; }
       }
     }
-    if (variant == 1 && warps == 0)
+    if ((variant == 1 || variant == 3) && warps == 0)
       throw Error(ST_INVALID_ARGUMENT, "shared-memory variant requested but the PCFs do not fit in shared memory");
     if (warps > 0)
     {
       pl.smem = true;
+      pl.kvar = variant == 3 ? 1 : 2;
       pl.warps = warps;
       pl.lmax_c = lmax_c;
       pl.row_cap = row_cap;
@@ -193,6 +195,7 @@ namespace sbg
     else
     {
       pl.smem = false;
+      pl.kvar = 0;
       pl.warps = want_w > 0 ? std::min(want_w, 32) : 16;
       pl.lmax_c = lmax_c;
       pl.row_cap = 0;
@@ -337,7 +340,7 @@ namespace sbg
     L.lmax_c = pl.lmax_c;
     L.row_cap = pl.row_cap;
     const int grid = (int)std::min<uint64_t>((uint64_t)pl.grid, d.n_items);
-    SBG_CUDA(launch_pairs<T>(L, opk, pl.smem, pl.warps, grid, pl.smem_bytes, st));
+    SBG_CUDA(launch_pairs<T>(L, opk, pl.kvar, pl.warps, grid, pl.smem_bytes, st));
   }
 
   template <typename T>

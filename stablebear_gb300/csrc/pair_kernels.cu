@@ -7,6 +7,8 @@
 
 namespace sbg
 {
+  constexpr int kUnrollConst = 8;  // rectangles per naive block sum (Kahan across blocks)
+
   namespace
   {
     constexpr unsigned FULL = 0xffffffffu;
@@ -94,12 +96,45 @@ namespace sbg
     return PairOp<K>::fin(acc - comp, p);
   }
 
+  // The same merge with both sides in the dynamic shared array, addressed by
+  // 32-bit element indices (row element fi, column element gi*32 + lane).
+  template <typename T, int K, int U>
+  __device__ __forceinline__ T merge_smem_idx(const Elem<T>* __restrict__ sm, uint32_t fi, uint32_t gi,
+                                              uint32_t steps, T p)
+  {
+    Elem<T> F = sm[fi];
+    Elem<T> G = sm[gi];
+    T t = T(0), acc = T(0), comp = T(0);
+    const uint32_t nblk = (steps + U - 1) / U;
+    for (uint32_t b = 0; b < nblk; ++b)
+    {
+      T blk = T(0);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+      {
+        const bool takeF = F.tn <= G.tn;
+        const T tn = takeF ? F.tn : G.tn;
+        blk += PairOp<K>::seg(tn - t, F.v, G.v, p);
+        t = tn;
+        fi += takeF ? 1u : 0u;
+        gi += takeF ? 0u : 32u;
+        F = sm[fi];
+        G = sm[gi];
+      }
+      kahan_add(acc, comp, blk);
+    }
+    return PairOp<K>::fin(acc - comp, p);
+  }
+
   // Persistent kernel.  SMEM = true stages the item's 32 columns and each
   // warp's row in shared memory; SMEM = false reads the packed segment layout
   // (pack_segments_kernel) from global memory through L1.
-  template <typename T, int K, int U, bool SMEM>
+  // VAR: 0 global-memory variant, 1 shared memory (pointer walk), 2 shared
+  // memory (32-bit index walk).
+  template <typename T, int K, int U, int VAR>
   __global__ void __launch_bounds__(1024, 1) pairs_kernel(const __grid_constant__ LaunchParams<T> L)
   {
+    constexpr bool SMEM = VAR != 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Elem<T>* cols = reinterpret_cast<Elem<T>*>(smem_raw);
     Elem<T>* rows = cols + (size_t)L.lmax_c * 32;
@@ -212,7 +247,8 @@ namespace sbg
               rbuf[k].tn = TM;
             }
             __syncwarp();
-            res = merge_pair<T, K, U, 32, false>(rbuf, cols + lane, steps, rlen, p);
+            if (VAR == 1) res = merge_pair<T, K, U, 32, false>(rbuf, cols + lane, steps, rlen, p);
+            else res = merge_smem_idx<T, K, U>(cols, (uint32_t)(rbuf - cols), (uint32_t)lane, steps, p);
             __syncwarp();
           }
           else
@@ -262,20 +298,20 @@ namespace sbg
 
   // ---- launchers ------------------------------------------------------------
 
-  template <typename T, bool SMEM>
+  template <typename T, int VAR>
   static cudaError_t launch_op(int opk, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const LaunchParams<T>& L)
   {
-    constexpr int U = 8;
+    constexpr int U = kUnrollConst;
     void (*fn)(const LaunchParams<T>) = nullptr;
     switch (opk)
     {
-      case OPK_L1: fn = pairs_kernel<T, OPK_L1, U, SMEM>; break;
-      case OPK_L2DIST: fn = pairs_kernel<T, OPK_L2DIST, U, SMEM>; break;
-      case OPK_LP: fn = pairs_kernel<T, OPK_LP, U, SMEM>; break;
-      case OPK_INNER: fn = pairs_kernel<T, OPK_INNER, U, SMEM>; break;
+      case OPK_L1: fn = pairs_kernel<T, OPK_L1, U, VAR>; break;
+      case OPK_L2DIST: fn = pairs_kernel<T, OPK_L2DIST, U, VAR>; break;
+      case OPK_LP: fn = pairs_kernel<T, OPK_LP, U, VAR>; break;
+      case OPK_INNER: fn = pairs_kernel<T, OPK_INNER, U, VAR>; break;
       default: return cudaErrorInvalidValue;
     }
-    if (SMEM)
+    if (VAR != 0)
     {
       cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
@@ -285,12 +321,13 @@ namespace sbg
   }
 
   template <typename T>
-  cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, bool smem_variant, int warps, int grid,
+  cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, int variant, int warps, int grid,
                            size_t smem_bytes, cudaStream_t s)
   {
     dim3 g((unsigned)grid), b((unsigned)(warps * 32));
-    if (smem_variant) return launch_op<T, true>(opk, g, b, smem_bytes, s, L);
-    return launch_op<T, false>(opk, g, b, 0, s, L);
+    if (variant == 1) return launch_op<T, 1>(opk, g, b, smem_bytes, s, L);
+    if (variant == 2) return launch_op<T, 2>(opk, g, b, smem_bytes, s, L);
+    return launch_op<T, 0>(opk, g, b, 0, s, L);
   }
 
   template <typename T>
@@ -304,12 +341,10 @@ namespace sbg
     return cudaGetLastError();
   }
 
-  constexpr int kUnroll = 8;
-
-  template cudaError_t launch_pairs<float>(const LaunchParams<float>&, int, bool, int, int, size_t, cudaStream_t);
-  template cudaError_t launch_pairs<double>(const LaunchParams<double>&, int, bool, int, int, size_t, cudaStream_t);
+  template cudaError_t launch_pairs<float>(const LaunchParams<float>&, int, int, int, int, size_t, cudaStream_t);
+  template cudaError_t launch_pairs<double>(const LaunchParams<double>&, int, int, int, int, size_t, cudaStream_t);
   template cudaError_t launch_pack<float>(const float*, const uint64_t*, uint64_t, Elem<float>*, int, cudaStream_t);
   template cudaError_t launch_pack<double>(const double*, const uint64_t*, uint64_t, Elem<double>*, int, cudaStream_t);
 
-  int kernel_unroll() { return kUnroll; }
+  int kernel_unroll() { return kUnrollConst; }
 }

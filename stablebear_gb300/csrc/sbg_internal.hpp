@@ -65,7 +65,7 @@ namespace sbg
     // Engine knobs (0 = automatic).
     std::atomic<int> warps{0};
     std::atomic<int> rowChunk{0};        // Q: rows per work item = 32 * Q
-    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory, 2 global-memory
+    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory, 2 global-memory, 3 shared-memory pointer walk
     std::atomic<int> order{0};           // 0 auto, 1 caller order, 2 length-sorted
     std::atomic<uint64_t> bandBytes{0};  // output bytes per pipeline band (0 = auto)
   };
@@ -124,6 +124,7 @@ namespace sbg
   struct Plan
   {
     bool smem = true;
+    int kvar = 2;      // kernel variant: 0 global memory, 1 shared pointer walk, 2 shared index walk
     int warps = 16;
     int grid = 1;
     uint32_t q = 1;
@@ -148,7 +149,7 @@ namespace sbg
 
   // Kernel launchers (pair_kernels.cu).
   template <typename T>
-  cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, bool smem_variant, int warps, int grid,
+  cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, int variant, int warps, int grid,
                            size_t smem_bytes, cudaStream_t s);
   template <typename T>
   cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, int sms, cudaStream_t s);
