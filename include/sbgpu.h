@@ -95,6 +95,16 @@ int sbg_get_device_verbose(void);
  * by breakpoint count), output bytes per pipeline band. */
 int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes);
 
+/* How host-buffer entry points return results: 0 automatic (= 1), 1 device
+ * bands copied out through pinned staging buffers while the next band
+ * computes, 2 the kernel stores straight into the caller's host buffer
+ * (only on devices that use the host page tables, e.g. Grace + NVLink-C2C;
+ * SBG_ERR_INVALID_ARGUMENT elsewhere). */
+int sbg_set_output_mode(int mode);
+/* cudaDevAttrPageableMemoryAccess and ...UsesHostPageTables of the current
+ * device (both 1 where output mode 2 is available). */
+int sbg_host_memory_access(int* pageable, int* uses_host_page_tables);
+
 /* ---- tasks: the 12 factories of include/sbear/cuda/cuda_matrix_integrate_api.hpp:19-113
  *      and StoppableTask (include/sbear/task.hpp:15-172) ------------------------ */
 

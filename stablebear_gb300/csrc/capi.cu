@@ -2,6 +2,7 @@
 // status codes plus a per-thread message.
 #include "../../include/sbgpu.h"
 #include "sbg_internal.hpp"
+#include "host_copy.hpp"
 
 #include <chrono>
 #include <condition_variable>
@@ -208,6 +209,21 @@ extern "C"
       settings().variant.store(variant);
       settings().order.store(order);
       settings().bandBytes.store(band_bytes);
+    });
+  }
+
+  int sbg_set_output_mode(int mode)
+  {
+    if (mode < 0 || mode > 2) { set_last_error("output mode must be 0, 1 or 2"); return SBG_ERR_INVALID_ARGUMENT; }
+    settings().outputMode.store(mode);
+    return SBG_OK;
+  }
+
+  int sbg_host_memory_access(int* pageable, int* uses_host_page_tables)
+  {
+    return guarded([&] {
+      (void)current_device();
+      host_memory_access(pageable, uses_host_page_tables);
     });
   }
 

@@ -11,6 +11,7 @@
 //   * bands alternate between two device buffers so the copy of band b
 //     overlaps the kernel of band b + 1.
 #include "sbg_internal.hpp"
+#include "host_copy.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -508,15 +509,32 @@ namespace sbg
     const Plan pl = make_plan<T>(mode, rows.n, cs.n, rstat, cstat, dev);
     const uint64_t chunk_rows = 32ull * pl.q;
 
+    // Output route.  Direct: on coherent hosts (Grace + NVLink-C2C, where the
+    // device walks the host page tables) the kernel stores straight into the
+    // caller's matrix, one launch, no device output buffer and no copies.
+    // Staged: bands of whole row chunks into two device buffers, each band
+    // copied out while the next band computes (HostStager).
+    int out_mode = settings().outputMode.load();
+    bool direct = false;
+    if (out_mode == 2)
+    {
+      int pageable = 0, hpt = 0;
+      host_memory_access(&pageable, &hpt);
+      if (!(pageable && hpt))
+        throw Error(ST_INVALID_ARGUMENT, "direct host output needs a device that uses the host page tables");
+      direct = true;
+    }
+
     // Bands of whole row chunks.  One band when sorted (the permuted result
-    // is scattered over the whole matrix) or when the output is small.
+    // is scattered over the whole matrix), when writing directly, or when
+    // the output is small.
     uint64_t band_bytes = settings().bandBytes.load();
     if (band_bytes == 0) band_bytes = out_bytes > (512ull << 20) ? out_bytes / 8 + 1 : out_bytes;
     band_bytes = std::min<uint64_t>(band_bytes, budget / 2 > 0 ? budget / 2 : band_bytes);
     std::vector<std::pair<uint64_t, uint64_t>> bands;
-    if (sorted || band_bytes >= out_bytes)
+    if (direct || sorted || band_bytes >= out_bytes)
     {
-      if (out_bytes > budget) throw Error(ST_OUT_OF_MEMORY, "output does not fit in device memory");
+      if (!direct && out_bytes > budget) throw Error(ST_OUT_OF_MEMORY, "output does not fit in device memory");
       bands.emplace_back(0, rows.n);
     }
     else
@@ -539,7 +557,7 @@ namespace sbg
     uint64_t max_band = 0;
     for (auto& b : bands)
       max_band = std::max<uint64_t>(max_band, row_output_start(mode, b.second, cs.n) - row_output_start(mode, b.first, cs.n));
-    const int nbuf = bands.size() > 1 ? 2 : 1;
+    const int nbuf = direct ? 0 : (bands.size() > 1 ? 2 : 1);
     DeviceBuffer obuf[2];
     for (int b = 0; b < nbuf; ++b) obuf[b].reset(std::max<uint64_t>(1, max_band) * sizeof(T));
     EventGuard computed[2], copied[2];
@@ -571,9 +589,9 @@ namespace sbg
       d.cpts = kc_pts; d.coff = (mode == MODE_CROSS) ? dcols.view.off : drows.view.off; d.nc = cs.n;
       d.rperm = sorted ? drperm.as<uint32_t>() : nullptr;
       d.cperm = sorted ? (mode == MODE_CROSS ? dcperm.as<uint32_t>() : drperm.as<uint32_t>()) : nullptr;
-      d.out = obuf[b].as<T>();
-      d.out_base = sorted ? 0 : row_output_start(mode, bands[k].first, cs.n);
-      d.out_count = sorted ? total : row_output_start(mode, bands[k].second, cs.n) - d.out_base;
+      d.out = direct ? out : obuf[b].as<T>();
+      d.out_base = (sorted || direct) ? 0 : row_output_start(mode, bands[k].first, cs.n);
+      d.out_count = (sorted || direct) ? total : row_output_start(mode, bands[k].second, cs.n) - d.out_base;
       d.ld = cs.n;
       d.row_begin = bands[k].first; d.row_end = bands[k].second;
       d.q = pl.q; d.mode = mode; d.p = (T)p;
@@ -582,6 +600,14 @@ namespace sbg
     };
 
     bool cancelled = false;
+    if (direct)
+    {
+      launch_band(0);
+      SBG_CUDA(cudaStreamSynchronize(compute.s));
+      if (ctl.progress) ctl.progress(total);
+      return;
+    }
+    HostStager stager(std::min<uint64_t>(std::max<uint64_t>(max_band * sizeof(T), 1), 256ull << 20));
     launch_band(0);
     for (size_t k = 0; k < bands.size(); ++k)
     {
@@ -591,13 +617,13 @@ namespace sbg
       const uint64_t lo = sorted ? 0 : row_output_start(mode, rb, cs.n);
       const uint64_t hi = sorted ? total : row_output_start(mode, re, cs.n);
       SBG_CUDA(cudaStreamWaitEvent(copy.s, computed[b].e, 0));
-      if (hi > lo)
-        SBG_CUDA(cudaMemcpyAsync(out + lo, obuf[b].as<T>(), (hi - lo) * sizeof(T), cudaMemcpyDeviceToHost, copy.s));
+      if (hi > lo) stager.copy(out + lo, obuf[b].as<T>(), (hi - lo) * sizeof(T), copy.s);
+      stager.flush();
       SBG_CUDA(cudaEventRecord(copied[b].e, copy.s));
-      SBG_CUDA(cudaEventSynchronize(copied[b].e));
       if (ctl.progress) ctl.progress(hi - lo);
       if (ctl.stop && ctl.stop->load()) { cancelled = true; break; }
     }
+    stager.flush();
     SBG_CUDA(cudaStreamSynchronize(compute.s));
     SBG_CUDA(cudaStreamSynchronize(copy.s));
     if (cancelled) throw Error(ST_CANCELLED, "task was cancelled");

@@ -96,14 +96,45 @@ namespace sbg
     return PairOp<K>::fin(acc - comp, p);
   }
 
-  // The same merge with both sides in the dynamic shared array, addressed by
-  // 32-bit element indices (row element fi, column element gi*32 + lane).
-  template <typename T, int K, int U>
-  __device__ __forceinline__ T merge_smem_idx(const Elem<T>* __restrict__ sm, uint32_t fi, uint32_t gi,
-                                              uint32_t steps, T p)
+  // Advance exactly one side of the merge with predicated shared-memory
+  // loads: only the side whose next breakpoint comes first (the row on a
+  // tie) moves its 32-bit shared address and reloads its element; the other
+  // side issues no load.  This halves the shared-memory bytes per step of the
+  // plain two-load walk, which is what bounds the kernel (one new 8-byte
+  // element per lane per step is the floor).
+  __device__ __forceinline__ void advance_shared(float& fv, float& ft, float& gv, float& gt, uint32_t& af,
+                                                 uint32_t& ag)
   {
-    Elem<T> F = sm[fi];
-    Elem<T> G = sm[gi];
+    asm("{\n\t.reg .pred p;\n\t"
+        "setp.le.f32 p, %1, %3;\n\t"
+        "@p add.u32 %4, %4, 8;\n\t"
+        "@!p add.u32 %5, %5, 256;\n\t"
+        "@p ld.shared.v2.f32 {%0, %1}, [%4];\n\t"
+        "@!p ld.shared.v2.f32 {%2, %3}, [%5];\n\t}"
+        : "+f"(fv), "+f"(ft), "+f"(gv), "+f"(gt), "+r"(af), "+r"(ag));
+  }
+
+  __device__ __forceinline__ void advance_shared(double& fv, double& ft, double& gv, double& gt, uint32_t& af,
+                                                 uint32_t& ag)
+  {
+    asm("{\n\t.reg .pred p;\n\t"
+        "setp.le.f64 p, %1, %3;\n\t"
+        "@p add.u32 %4, %4, 16;\n\t"
+        "@!p add.u32 %5, %5, 512;\n\t"
+        "@p ld.shared.v2.f64 {%0, %1}, [%4];\n\t"
+        "@!p ld.shared.v2.f64 {%2, %3}, [%5];\n\t}"
+        : "+d"(fv), "+d"(ft), "+d"(gv), "+d"(gt), "+r"(af), "+r"(ag));
+  }
+
+  // Shared-memory merge with predicated loads.  pf: the warp's row buffer,
+  // pg: this lane's column in the interleaved column block (stride 32).
+  template <typename T, int K, int U>
+  __device__ __forceinline__ T merge_smem_pred(const Elem<T>* pf, const Elem<T>* pg, uint32_t steps, T p)
+  {
+    Elem<T> F = *pf;
+    Elem<T> G = *pg;
+    uint32_t af = (uint32_t)__cvta_generic_to_shared(pf);
+    uint32_t ag = (uint32_t)__cvta_generic_to_shared(pg);
     T t = T(0), acc = T(0), comp = T(0);
     const uint32_t nblk = (steps + U - 1) / U;
     for (uint32_t b = 0; b < nblk; ++b)
@@ -112,14 +143,10 @@ namespace sbg
 #pragma unroll
       for (int u = 0; u < U; ++u)
       {
-        const bool takeF = F.tn <= G.tn;
-        const T tn = takeF ? F.tn : G.tn;
+        const T tn = fmin(F.tn, G.tn);
         blk += PairOp<K>::seg(tn - t, F.v, G.v, p);
         t = tn;
-        fi += takeF ? 1u : 0u;
-        gi += takeF ? 0u : 32u;
-        F = sm[fi];
-        G = sm[gi];
+        advance_shared(F.v, F.tn, G.v, G.tn, af, ag);
       }
       kahan_add(acc, comp, blk);
     }
@@ -129,8 +156,8 @@ namespace sbg
   // Persistent kernel.  SMEM = true stages the item's 32 columns and each
   // warp's row in shared memory; SMEM = false reads the packed segment layout
   // (pack_segments_kernel) from global memory through L1.
-  // VAR: 0 global-memory variant, 1 shared memory (pointer walk), 2 shared
-  // memory (32-bit index walk).
+  // VAR: 0 global-memory variant, 1 shared memory with a two-load pointer
+  // walk, 2 shared memory with predicated one-side loads (the default).
   template <typename T, int K, int U, int VAR>
   __global__ void __launch_bounds__(1024, 1) pairs_kernel(const __grid_constant__ LaunchParams<T> L)
   {
@@ -248,7 +275,7 @@ namespace sbg
             }
             __syncwarp();
             if (VAR == 1) res = merge_pair<T, K, U, 32, false>(rbuf, cols + lane, steps, rlen, p);
-            else res = merge_smem_idx<T, K, U>(cols, (uint32_t)(rbuf - cols), (uint32_t)lane, steps, p);
+            else res = merge_smem_pred<T, K, U>(rbuf, cols + lane, steps, p);
             __syncwarp();
           }
           else

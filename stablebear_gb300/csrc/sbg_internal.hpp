@@ -68,6 +68,7 @@ namespace sbg
     std::atomic<int> variant{0};         // 0 auto, 1 shared-memory, 2 global-memory, 3 shared-memory pointer walk
     std::atomic<int> order{0};           // 0 auto, 1 caller order, 2 length-sorted
     std::atomic<uint64_t> bandBytes{0};  // output bytes per pipeline band (0 = auto)
+    std::atomic<int> outputMode{0};      // host results: 0 auto (staged), 1 staged copy, 2 direct stores (coherent hosts)
   };
   Settings& settings();
 
@@ -124,7 +125,7 @@ namespace sbg
   struct Plan
   {
     bool smem = true;
-    int kvar = 2;      // kernel variant: 0 global memory, 1 shared pointer walk, 2 shared index walk
+    int kvar = 2;      // kernel variant: 0 global memory, 1 shared two-load walk, 2 shared predicated walk
     int warps = 16;
     int grid = 1;
     uint32_t q = 1;
