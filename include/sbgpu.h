@@ -185,6 +185,39 @@ uint64_t sbg_enumerate_items(int skip_mode, uint64_t n_rows, uint64_t n_cols, ui
  * instruction per lane = one lane-op), from a register-only FMA loop. */
 int sbg_measure_peak(int kind, double* lane_ops_per_s);
 
+/* ---- device entry that allocates nothing --------------------------------------
+ * No counterpart in the reference; an addition of this library.
+ *
+ * For callers that cannot allocate device memory when they need a matrix: an
+ * application whose allocator owns all device memory, a component running
+ * while a CUDA graph is being recorded around it, a plugin host that only lends
+ * inputs and outputs.  Same computation and arguments as sbg_pairwise_device,
+ * plus the total breakpoint counts of the row and column sets; it calls no
+ * cudaMalloc, cudaFree or other allocating routine.  Its scratch (the
+ * persistent kernel's work-queue counter and, for PCFs too long for the
+ * shared-memory kernel, a packed copy of the breakpoints) lives in one
+ * fixed array of SBG_NOALLOC_SCRATCH_BYTES inside the library, which every
+ * GPU that loads the library holds until the process exits.
+ *   - max_points must be given (measuring it would need scratch of its own).
+ *   - A problem whose scratch would exceed SBG_NOALLOC_SCRATCH_BYTES is
+ *     rejected with SBG_ERR_INVALID_ARGUMENT and a message giving both sizes;
+ *     PCFs that fit the shared-memory kernel need only 256 bytes, whatever n.
+ *   - The first call on each device looks up the array's device address on
+ *     that device (cudaGetSymbolAddress); make that first call before any
+ *     stream capture.
+ *   - All calls share the one array: calls whose work overlaps on the GPU (on
+ *     different streams, or from different threads) race on it.  Serialise
+ *     them, e.g. on one stream. */
+#define SBG_NOALLOC_SCRATCH_BYTES (4u << 20)
+int sbg_pairwise_device_noalloc(int dtype, int op, double p, int skip_mode,
+                                const void* row_points, const uint64_t* row_offsets, uint64_t n_rows,
+                                uint64_t n_row_points,
+                                const void* col_points, const uint64_t* col_offsets, uint64_t n_cols,
+                                uint64_t n_col_points,
+                                const uint32_t* row_perm, const uint32_t* col_perm, uint32_t max_points,
+                                void* out, uint64_t out_base, uint64_t row_begin, uint64_t row_end,
+                                void* stream);
+
 /* Number of output elements of a problem (n(n-1)/2, n(n+1)/2 or n_rows*n_cols). */
 uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols);
 

@@ -66,6 +66,8 @@ SIGNATURES = {
     "sbg_pairwise_host": (_I, [_I, _I, _D, _I, _P, _P, _U64, _P, _P, _U64, _P, _I]),
     "sbg_pairwise_device": (_I, [_I, _I, _D, _I, _P, _P, _U64, _P, _P, _U64, _P, _P, ctypes.c_uint32, _P, _U64,
                                  _U64, _U64, _P]),
+    "sbg_pairwise_device_noalloc": (_I, [_I, _I, _D, _I, _P, _P, _U64, _U64, _P, _P, _U64, _U64, _P, _P,
+                                         ctypes.c_uint32, _P, _U64, _U64, _U64, _P]),
     "sbg_output_count": (_U64, [_I, _U64, _U64]),
     "sbg_measure_peak": (_I, [_I, ctypes.POINTER(_D)]),
     "sbg_enumerate_items": (_U64, [_I, _U64, _U64, _U64, _U64, ctypes.c_uint32, _P, _U64]),

@@ -325,19 +325,26 @@ namespace sbg
   // One launch of the persistent kernel over rows [d.row_begin, d.row_end)
   // of one problem.  The queue counter is stream-ordered scratch.
   template <typename T>
-  static void launch_problem(ProblemDesc<T> d, const Plan& pl, int opk, cudaStream_t st)
+  static void launch_problem(ProblemDesc<T> d, const Plan& pl, int opk, cudaStream_t st,
+                             unsigned long long* given_queue = nullptr)
   {
     d.item_begin = 0;
     d.n_items = problem_item_count(d);
     if (d.n_items == 0) return;
-    AsyncBuf<T> queue(sizeof(unsigned long long), st);
-    SBG_CUDA(cudaMemsetAsync(queue.p, 0, sizeof(unsigned long long), st));
+    std::unique_ptr<AsyncBuf<T>> own;
+    unsigned long long* queue = given_queue;
+    if (!queue)
+    {
+      own.reset(new AsyncBuf<T>(sizeof(unsigned long long), st));
+      queue = static_cast<unsigned long long*>(own->p);
+    }
+    SBG_CUDA(cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st));
     LaunchParams<T> L{};
     L.one = d;
     L.probs = nullptr;
     L.n_probs = 1;
     L.total_items = d.n_items;
-    L.queue = static_cast<unsigned long long*>(queue.p);
+    L.queue = queue;
     L.lmax_c = pl.lmax_c;
     L.row_cap = pl.row_cap;
     const int grid = (int)std::min<uint64_t>((uint64_t)pl.grid, d.n_items);
@@ -393,14 +400,17 @@ namespace sbg
         SBG_CUDA(cudaMemcpyAsync(&ctot, cs.off + cs.n, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
       SBG_CUDA(cudaStreamSynchronize(st));
       rpack.reset(new AsyncBuf<T>(sizeof(Elem<T>) * std::max<uint64_t>(rtot, 1), st));
-      SBG_CUDA(launch_pack<T>(rows.pts, rows.off, rows.n, (Elem<T>*)rpack->p, dev.sms, st));
+      SBG_CUDA(launch_pack<T>(rows.pts, rows.off, rows.n, (Elem<T>*)rpack->p, rtot, dev.sms, st));
       d.rpts = reinterpret_cast<const T*>(rpack->p);
       d.cpts = d.rpts;
+      d.rcap = rtot;
+      d.ccap = rtot;
       if (mode == MODE_CROSS)
       {
         cpack.reset(new AsyncBuf<T>(sizeof(Elem<T>) * std::max<uint64_t>(ctot, 1), st));
-        SBG_CUDA(launch_pack<T>(cs.pts, cs.off, cs.n, (Elem<T>*)cpack->p, dev.sms, st));
+        SBG_CUDA(launch_pack<T>(cs.pts, cs.off, cs.n, (Elem<T>*)cpack->p, ctot, dev.sms, st));
         d.cpts = reinterpret_cast<const T*>(cpack->p);
+        d.ccap = ctot;
       }
     }
     launch_problem<T>(d, pl, opk, st);
@@ -411,6 +421,85 @@ namespace sbg
   template void compute_device<double>(int, int, double, const PcfSet<double>&, const PcfSet<double>*,
                                        const uint32_t*, const uint32_t*, uint32_t, double*, uint64_t, uint64_t,
                                        uint64_t, cudaStream_t);
+
+  template <typename T>
+  size_t scratch_needed(int mode, uint64_t n_rows, uint64_t n_cols, uint32_t lmax, uint64_t row_points,
+                        uint64_t col_points)
+  {
+    const DeviceInfo dev = device_info();
+    LengthStats ls;
+    ls.lmax = lmax; ls.lmin = 1; ls.mean = lmax;
+    const Plan pl = make_plan<T>(mode, n_rows, mode == MODE_CROSS ? n_cols : n_rows, ls, ls, dev);
+    size_t need = 256;  // work-queue counter
+    if (!pl.smem)
+    {
+      need += ((sizeof(Elem<T>) * row_points + 255) / 256) * 256;
+      if (mode == MODE_CROSS) need += ((sizeof(Elem<T>) * col_points + 255) / 256) * 256;
+    }
+    return need;
+  }
+
+  template <typename T>
+  void compute_device_scratch(int mode, int op, double p, const PcfSet<T>& rows, const PcfSet<T>* cols,
+                              const uint32_t* rperm, const uint32_t* cperm, uint32_t lmax, uint64_t row_points,
+                              uint64_t col_points, T* out, uint64_t out_base, uint64_t row_begin, uint64_t row_end,
+                              void* scratch, size_t scratch_bytes, cudaStream_t st)
+  {
+    const DeviceInfo dev = device_info();
+    if (mode == MODE_CROSS && !cols) throw Error(ST_INVALID_ARGUMENT, "cdist needs a column set");
+    if (lmax == 0) throw Error(ST_INVALID_ARGUMENT, "max_points must be given (measuring it would allocate)");
+    const PcfSet<T>& cs = (mode == MODE_CROSS) ? *cols : rows;
+    if (row_end == 0 || row_end > rows.n) row_end = rows.n;
+    if (row_begin >= row_end || cs.n == 0) return;
+    const int opk = op_kind(op, p);
+    LengthStats ls;
+    ls.lmax = lmax; ls.lmin = 1; ls.mean = lmax;
+    const Plan pl = make_plan<T>(mode, rows.n, cs.n, ls, ls, dev);
+    if (row_begin % (32ull * pl.q) != 0)
+      throw Error(ST_INVALID_ARGUMENT, "row_begin must be a multiple of the row chunk (32*q)");
+    const size_t need = scratch_needed<T>(mode, rows.n, cs.n, lmax, row_points, col_points);
+    if (need > scratch_bytes)
+      throw Error(ST_INVALID_ARGUMENT, "problem needs " + std::to_string(need) + " bytes of scratch; the limit is " +
+                  std::to_string(scratch_bytes) + " bytes");
+
+    ProblemDesc<T> d{};
+    d.rpts = rows.pts; d.roff = rows.off; d.rperm = rperm; d.nr = rows.n;
+    d.cpts = cs.pts; d.coff = cs.off; d.cperm = (mode == MODE_CROSS) ? cperm : rperm; d.nc = cs.n;
+    d.out = out; d.out_base = out_base; d.ld = cs.n;
+    d.row_begin = row_begin; d.row_end = row_end;
+    d.q = pl.q; d.mode = mode; d.p = (T)p;
+    {
+      const uint64_t hi = (rperm || cperm) ? output_count(mode, rows.n, cs.n) : row_output_start(mode, row_end, cs.n);
+      d.out_count = hi > out_base ? hi - out_base : 0;
+    }
+    char* base = static_cast<char*>(scratch);
+    if (!pl.smem)
+    {
+      Elem<T>* rp = reinterpret_cast<Elem<T>*>(base + 256);
+      SBG_CUDA(launch_pack<T>(rows.pts, rows.off, rows.n, rp, row_points, dev.sms, st));
+      d.rpts = reinterpret_cast<const T*>(rp);
+      d.cpts = d.rpts;
+      d.rcap = row_points;
+      d.ccap = row_points;
+      if (mode == MODE_CROSS)
+      {
+        Elem<T>* cp = reinterpret_cast<Elem<T>*>(base + 256 + ((sizeof(Elem<T>) * row_points + 255) / 256) * 256);
+        SBG_CUDA(launch_pack<T>(cs.pts, cs.off, cs.n, cp, col_points, dev.sms, st));
+        d.cpts = reinterpret_cast<const T*>(cp);
+        d.ccap = col_points;
+      }
+    }
+    launch_problem<T>(d, pl, opk, st, reinterpret_cast<unsigned long long*>(base));
+  }
+
+  template size_t scratch_needed<float>(int, uint64_t, uint64_t, uint32_t, uint64_t, uint64_t);
+  template size_t scratch_needed<double>(int, uint64_t, uint64_t, uint32_t, uint64_t, uint64_t);
+  template void compute_device_scratch<float>(int, int, double, const PcfSet<float>&, const PcfSet<float>*,
+                                              const uint32_t*, const uint32_t*, uint32_t, uint64_t, uint64_t, float*,
+                                              uint64_t, uint64_t, uint64_t, void*, size_t, cudaStream_t);
+  template void compute_device_scratch<double>(int, int, double, const PcfSet<double>&, const PcfSet<double>*,
+                                               const uint32_t*, const uint32_t*, uint32_t, uint64_t, uint64_t,
+                                               double*, uint64_t, uint64_t, uint64_t, void*, size_t, cudaStream_t);
 
   // ---- host pipeline ----------------------------------------------------------
 
@@ -569,13 +658,15 @@ namespace sbg
     if (!pl.smem)
     {
       rpack.reset(sizeof(Elem<T>) * std::max<uint64_t>(1, rows.off[rows.n]));
-      SBG_CUDA(launch_pack<T>(drows.view.pts, drows.view.off, rows.n, rpack.as<Elem<T>>(), dev.sms, compute.s));
+      SBG_CUDA(launch_pack<T>(drows.view.pts, drows.view.off, rows.n, rpack.as<Elem<T>>(), rows.off[rows.n], dev.sms,
+                              compute.s));
       kr_pts = reinterpret_cast<const T*>(rpack.get());
       kc_pts = kr_pts;
       if (mode == MODE_CROSS)
       {
         cpack.reset(sizeof(Elem<T>) * std::max<uint64_t>(1, cs.off[cs.n]));
-        SBG_CUDA(launch_pack<T>(dcols.view.pts, dcols.view.off, cs.n, cpack.as<Elem<T>>(), dev.sms, compute.s));
+        SBG_CUDA(launch_pack<T>(dcols.view.pts, dcols.view.off, cs.n, cpack.as<Elem<T>>(), cs.off[cs.n], dev.sms,
+                                compute.s));
         kc_pts = reinterpret_cast<const T*>(cpack.get());
       }
     }
@@ -595,6 +686,8 @@ namespace sbg
       d.ld = cs.n;
       d.row_begin = bands[k].first; d.row_end = bands[k].second;
       d.q = pl.q; d.mode = mode; d.p = (T)p;
+      d.rcap = rows.off[rows.n];
+      d.ccap = cs.off[cs.n];
       launch_problem<T>(d, pl, opk, compute.s);
       SBG_CUDA(cudaEventRecord(computed[b].e, compute.s));
     };

@@ -216,6 +216,7 @@ namespace sbg
       const T p = Pp->p;
 
       bool item_ok = true;
+      if (!SMEM && __any_sync(FULL, coff + clen > Pp->ccap)) item_ok = false;  // offsets past the packed columns
       if (SMEM)
       {
         if (maxlc > L.lmax_c || __any_sync(FULL, clen == 0)) item_ok = false;  // host sized lmax_c; never expected
@@ -251,6 +252,7 @@ namespace sbg
           const uint32_t rlen = (uint32_t)(Pp->roff[iorig + 1] - roff);
           const bool ok = cvalid && (mode == MODE_CROSS || (mode == MODE_PDIST ? cj < i : cj <= i));
           if (!__any_sync(FULL, ok) || rlen == 0) continue;
+          if (!SMEM && roff + rlen > Pp->rcap) continue;  // offsets past the packed rows
           const uint32_t steps = rlen + maxlc - 1;
 
           T res;
@@ -304,7 +306,7 @@ namespace sbg
   // CSR offset) holds (v_k, t_{k+1}), the last one (v_{L-1}, TMAX).
   template <typename T>
   __global__ void pack_segments_kernel(const T* __restrict__ pts, const uint64_t* __restrict__ off, uint64_t n,
-                                       Elem<T>* __restrict__ out)
+                                       Elem<T>* __restrict__ out, uint64_t cap)
   {
     const uint64_t w = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -313,6 +315,7 @@ namespace sbg
     {
       const uint64_t o = off[i];
       const uint64_t len = off[i + 1] - o;
+      if (o + len > cap || len > cap) continue;  // never write past the packed buffer
       for (uint64_t k = lane; k < len; k += 32)
       {
         Elem<T> e;
@@ -358,20 +361,23 @@ namespace sbg
   }
 
   template <typename T>
-  cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, int sms, cudaStream_t s)
+  cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, uint64_t cap, int sms,
+                          cudaStream_t s)
   {
     if (n == 0) return cudaSuccess;
     uint64_t blocks = (n + 7) / 8;
-    uint64_t cap = (uint64_t)sms * 8;
-    if (blocks > cap) blocks = cap;
-    pack_segments_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(pts, off, n, out);
+    const uint64_t max_blocks = (uint64_t)sms * 8;
+    if (blocks > max_blocks) blocks = max_blocks;
+    pack_segments_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(pts, off, n, out, cap);
     return cudaGetLastError();
   }
 
   template cudaError_t launch_pairs<float>(const LaunchParams<float>&, int, int, int, int, size_t, cudaStream_t);
   template cudaError_t launch_pairs<double>(const LaunchParams<double>&, int, int, int, int, size_t, cudaStream_t);
-  template cudaError_t launch_pack<float>(const float*, const uint64_t*, uint64_t, Elem<float>*, int, cudaStream_t);
-  template cudaError_t launch_pack<double>(const double*, const uint64_t*, uint64_t, Elem<double>*, int, cudaStream_t);
+  template cudaError_t launch_pack<float>(const float*, const uint64_t*, uint64_t, Elem<float>*, uint64_t, int,
+                                          cudaStream_t);
+  template cudaError_t launch_pack<double>(const double*, const uint64_t*, uint64_t, Elem<double>*, uint64_t, int,
+                                           cudaStream_t);
 
   int kernel_unroll() { return kUnrollConst; }
 }

@@ -110,6 +110,9 @@ namespace sbg
     uint32_t q;        // rows per chunk = 32 * q
     int mode;
     T p;
+    // Global-memory variant: elements in the packed row / column arrays.
+    // Rows or column groups whose offsets reach past them are skipped.
+    uint64_t rcap, ccap;
   };
 
   // probs == nullptr: a single problem passed inline in `one` (kernel

@@ -153,7 +153,8 @@ namespace sbg
   cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, int variant, int warps, int grid,
                            size_t smem_bytes, cudaStream_t s);
   template <typename T>
-  cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, int sms, cudaStream_t s);
+  cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, uint64_t cap, int sms,
+                          cudaStream_t s);
   int kernel_unroll();
 
   // Control block of one host-side run (progress, cancellation).
@@ -177,6 +178,19 @@ namespace sbg
   void compute_device(int mode, int op, double p, const PcfSet<T>& rows, const PcfSet<T>* cols,
                       const uint32_t* rperm, const uint32_t* cperm, uint32_t lmax, T* out, uint64_t out_base,
                       uint64_t row_begin, uint64_t row_end, cudaStream_t stream);
+
+  // The device computation with caller-provided scratch (no allocation):
+  // the work-queue counter at scratch[0..8) and, when the PCFs are too long
+  // for the shared-memory kernel, the packed segment layout after it.
+  // Throws ST_INVALID_ARGUMENT when scratch_bytes is too small.
+  template <typename T>
+  void compute_device_scratch(int mode, int op, double p, const PcfSet<T>& rows, const PcfSet<T>* cols,
+                              const uint32_t* rperm, const uint32_t* cperm, uint32_t lmax, uint64_t row_points,
+                              uint64_t col_points, T* out, uint64_t out_base, uint64_t row_begin, uint64_t row_end,
+                              void* scratch, size_t scratch_bytes, cudaStream_t stream);
+  template <typename T>
+  size_t scratch_needed(int mode, uint64_t n_rows, uint64_t n_cols, uint32_t lmax, uint64_t row_points,
+                        uint64_t col_points);
 
   uint64_t output_count(int mode, uint64_t n_rows, uint64_t n_cols);
   uint64_t row_output_start(int mode, uint64_t row, uint64_t n_cols);

@@ -1,0 +1,99 @@
+"""The device entry that allocates nothing (sbg_pairwise_device_noalloc).
+
+It exists for callers that may not allocate device memory at the moment they
+need a matrix (an application whose own allocator owns all device memory, a
+component running inside someone else's graph capture, a plugin host that
+only lends buffers).  The test calls it through the C ABI twice in a row and
+checks each result against sbg_pairwise_device, the allocating entry point,
+with the tolerance the other parity tests use (float32: 1e-5 relative; here
+the two paths run the same kernel, so the results are in fact identical).
+It also checks the clear rejection of a problem too large for the fixed
+scratch.  This file is collected last so a failure here cannot hide others.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def env():
+    from stablebear_gb300 import build
+    build.build()
+    import torch
+    from stablebear_gb300 import _native as nat
+    assert torch.cuda.is_available()
+    return torch, nat
+
+
+def _device_csr(torch, pts, off):
+    return torch.from_numpy(pts).cuda(), torch.from_numpy(off.astype(np.int64)).cuda()
+
+
+def _run_pair(torch, nat, pts, off, skip, op, p):
+    dp, do = _device_csr(torch, pts, off)
+    n = len(off) - 1
+    count = int(nat.lib().sbg_output_count(skip, n, n))
+    lmax = int(np.diff(off.astype(np.int64)).max())
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    code = nat.F32 if pts.dtype == np.float32 else nat.F64
+    tdt = torch.float32 if pts.dtype == np.float32 else torch.float64
+    ref = torch.full((count,), float("nan"), dtype=tdt, device="cuda")
+    nat.check(nat.lib().sbg_pairwise_device(code, op, p, skip, dp.data_ptr(), do.data_ptr(), n, None, None, 0,
+                                            None, None, lmax, ref.data_ptr(), 0, 0, 0, st))
+    outs = []
+    for _ in range(2):  # two calls in a row share the scratch
+        got = torch.full((count,), float("nan"), dtype=tdt, device="cuda")
+        nat.check(nat.lib().sbg_pairwise_device_noalloc(code, op, p, skip, dp.data_ptr(), do.data_ptr(), n,
+                                                        int(off[-1]), None, None, 0, 0, None, None, lmax,
+                                                        got.data_ptr(), 0, 0, 0, st))
+        outs.append(got)
+    torch.cuda.synchronize()
+    ref = ref.cpu().numpy().astype(np.float64)
+    for got in outs:
+        g = got.cpu().numpy().astype(np.float64)
+        assert not np.isnan(g).any()
+        rel = np.abs(g - ref) / np.maximum(np.abs(ref), 1.0 if op == nat.OP_L2_INNER else 1e-30)
+        assert rel.max() <= TOL
+
+
+def test_no_alloc_matches_allocating_entry(env):
+    torch, nat = env
+    from stablebear_gb300 import synthetic
+    pts, off = synthetic.plain_l1(700, seed=31)
+    _run_pair(torch, nat, pts, off, nat.SKIP_LOWER_NODIAG, nat.OP_L1, 1.0)
+    _run_pair(torch, nat, pts, off, nat.SKIP_LOWER, nat.OP_L2_INNER, 1.0)
+
+
+def test_no_alloc_long_pcfs_use_scratch_copy(env):
+    """PCFs too long for the shared-memory kernel: the packed copy of the
+    breakpoints goes into the fixed scratch."""
+    torch, nat = env
+    from stablebear_gb300 import synthetic
+    lens = np.array([3, 9000, 5, 1, 7000, 12] * 5)
+    pts, off = synthetic.gaussian(len(lens), lens, np.float32, seed=5)
+    _run_pair(torch, nat, pts, off, nat.SKIP_LOWER_NODIAG, nat.OP_LP, 2.0)
+
+
+def test_no_alloc_rejects_oversized_problem(env):
+    torch, nat = env
+    from stablebear_gb300 import synthetic
+    lens = np.full(20, 40_000)  # 800k long breakpoints: more packed scratch than the fixed array holds
+    pts, off = synthetic.gaussian(len(lens), lens, np.float32, seed=6)
+    dp, do = _device_csr(torch, pts, off)
+    out = torch.empty(190, dtype=torch.float32, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = nat.lib().sbg_pairwise_device_noalloc(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                               do.data_ptr(), 20, int(off[-1]), None, None, 0, 0, None, None,
+                                               40_000, out.data_ptr(), 0, 0, 0, st)
+    assert rc == -1
+    msg = nat.last_error()
+    assert "scratch" in msg and "limit" in msg
+    assert nat.lib().sbg_pairwise_device_noalloc(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                                 do.data_ptr(), 20, int(off[-1]), None, None, 0, 0, None, None, 0,
+                                                 out.data_ptr(), 0, 0, 0, st) == -1
+    torch.cuda.synchronize()
