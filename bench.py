@@ -44,7 +44,129 @@ def parse():
     ap.add_argument("--cpu-sample-rows", type=int, default=0, help="rows in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="large", choices=["large", "plain", "stable_rank", "batched"],
+                    help="large: the headline workload; the others print their own report line")
     return ap.parse_args()
+
+
+# ---- the other workloads (reported beside the headline) -----------------------
+
+def _time_device(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def _device_problem(pts, off):
+    import torch
+    return torch.from_numpy(pts).cuda(), torch.from_numpy(off.astype(np.int64)).cuda()
+
+
+def run_aux(args):
+    import torch
+    from stablebear_gb300 import _native as nat, synthetic
+    from oracle import oracle as orc
+    lib = nat.lib()
+    st = lambda: ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    threads = os.cpu_count() or 1
+    rep = {"config_name": args.config, "data": "synthetic"}
+
+    def single(pts, off, opc, p, skip, out, lmax):
+        dp, do = _device_problem(pts, off)
+        n = len(off) - 1
+        return lambda: nat.check(lib.sbg_pairwise_device(nat.F32 if pts.dtype == np.float32 else nat.F64, opc, p, skip,
+                                                         dp.data_ptr(), do.data_ptr(), n, None, None, 0, None, None,
+                                                         lmax, out.data_ptr(), 0, 0, 0, st()))
+
+    if args.config == "plain":
+        pts, off = synthetic.plain_l1(1000, seed=0)
+        n = 1000
+        out = torch.empty(n * (n - 1) // 2, device="cuda")
+        f = single(pts, off, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, out, int(np.diff(off.astype(np.int64)).max()))
+        ms = _time_device(f, max(args.steps, 20), max(args.warmup, 3))
+        ref = orc.evaluate(pts, off, threads=threads)
+        t0 = time.perf_counter()
+        orc.evaluate(pts, off, threads=threads)
+        cpu_s = time.perf_counter() - t0
+        rep.update({"workload": "L1 pdist N=1000 f32, L~U{10..200}", "pairs": n * (n - 1) // 2,
+                    "gpu_ms": ms, "gpu_pairs_per_s": n * (n - 1) / 2 / (ms / 1e3),
+                    "segments": synthetic.segment_count(off, pts, 1),
+                    "cpu_pairs_per_s": n * (n - 1) / 2 / cpu_s, "cpu_cores": threads,
+                    "max_rel_err_vs_reference_cpu": float(np.max(np.abs(out.cpu().numpy() - ref) / np.maximum(np.abs(ref), 1e-30)))})
+    elif args.config == "stable_rank":
+        n = args.n if args.n != 100_000 else 20_000
+        pts, off = synthetic.stable_rank(n, seed=0)
+        lmax = int(np.diff(off.astype(np.int64)).max())
+        rows = np.unique(np.random.default_rng(1).integers(1, n, size=24)).astype(np.uint64)
+        for name, opc, p, skip in (("l2_kernel", nat.OP_L2_INNER, 1.0, nat.SKIP_LOWER),
+                                   ("l2_pdist", nat.OP_LP, 2.0, nat.SKIP_LOWER_NODIAG)):
+            cnt = int(lib.sbg_output_count(skip, n, n))
+            out = torch.empty(cnt, dtype=torch.float64, device="cuda")
+            f = single(pts, off, opc, p, skip, out, lmax)
+            ms = _time_device(f, max(1, args.steps // 2), 1)
+            mode = orc.MODE_KERNEL if skip == nat.SKIP_LOWER else orc.MODE_PDIST
+            oop = orc.OP_L2 if skip == nat.SKIP_LOWER else orc.OP_LP
+            t0 = time.perf_counter()
+            vals, starts = orc.evaluate_rows(pts, off, rows, op=oop, p=p, mode=mode, threads=threads)
+            cpu_s = time.perf_counter() - t0
+            truth, _ = orc.evaluate_rows(pts, off, rows[:6], op=oop, p=p, mode=mode, truth=True, threads=threads)
+            host = out.cpu().numpy()
+            per = 1 if skip == nat.SKIP_LOWER else 0
+            got = np.concatenate([host[(int(i) * (int(i) + 1) // 2 if per else int(i) * (int(i) - 1) // 2):
+                                       (int(i) * (int(i) + 1) // 2 if per else int(i) * (int(i) - 1) // 2) + int(i) + per]
+                                  for i in rows])
+            gt = got[: int(starts[min(6, len(rows))])]
+            floor = 1.0 if skip == nat.SKIP_LOWER else 1e-300
+            rep[name] = {"gpu_ms": ms, "pairs": cnt, "gpu_pairs_per_s": cnt / (ms / 1e3),
+                         "segments": synthetic.segment_count(off, pts, 2 if per else 1),
+                         "cpu_pairs_per_s": int(starts[-1]) / cpu_s, "cpu_cores": threads,
+                         "max_rel_err_vs_reference_cpu": float(np.max(np.abs(got - vals) / np.maximum(np.abs(vals), floor))),
+                         "max_rel_err_vs_fp64_oracle": float(np.max(np.abs(gt - truth) / np.maximum(np.abs(truth), floor)))}
+            del out
+        rep.update({"workload": f"N={n} f64 stable-rank-like, L=round(exp(U[ln16,ln4096]))", "lmax": lmax})
+    elif args.config == "batched":
+        from stablebear_gb300.batch import PairwiseBatch
+        probs = synthetic.batched_betti(512, seed=0)
+        pairs = sum((len(o) - 1) * (len(o) - 2) // 2 for _, o in probs)
+        segs = sum(synthetic.segment_count(o, p_, 1) for p_, o in probs)
+        for name, op, p in (("l1", "l1", 1.0), ("l2", "lp", 2.0)):
+            b = PairwiseBatch(probs, op=op, p=p, graph=True)
+            b.run()
+            torch.cuda.synchronize()
+            tuned = b.autotune()
+            ms_b = _time_device(b.run, max(3, args.steps), 2)
+            info = b.info()
+            # the plain single-problem path, one launch per problem
+            outs = [o for o in b.outputs]
+            fns = [single(pp, oo, nat.OP_L1 if op == "l1" else nat.OP_LP, p, nat.SKIP_LOWER_NODIAG, out_,
+                          int(np.diff(oo.astype(np.int64)).max())) for (pp, oo), out_ in zip(probs, outs)]
+            ms_plain = _time_device(lambda: [f() for f in fns], 2, 1)
+            # parity: two problems against the oracle
+            errs = []
+            b.run()
+            torch.cuda.synchronize()
+            for k in (0, 255):
+                pp, oo = probs[k]
+                want = orc.evaluate(pp, oo, op=orc.OP_L1 if op == "l1" else orc.OP_LP, p=p, threads=threads)
+                got = b.outputs[k].cpu().numpy()
+                errs.append(float(np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-30))))
+            rep[name] = {"batched_ms": ms_b, "batched_pairs_per_s": pairs / (ms_b / 1e3),
+                         "batched_segments_per_s": segs / (ms_b / 1e3), "plain_loop_ms": ms_plain,
+                         "plain_loop_pairs_per_s": pairs / (ms_plain / 1e3), "speedup_vs_plain": ms_plain / ms_b,
+                         "autotuned_ms": tuned, "launch": info, "max_rel_err_vs_reference_cpu": max(errs)}
+            b.close()
+        rep.update({"workload": "512 problems, N_i~U{50..2000}, L~U{8..1024}, f32 Betti-like", "pairs": pairs,
+                    "segments": segs})
+    print(json.dumps(rep), flush=True)
 
 
 def dist_env():
@@ -181,6 +303,10 @@ def main():
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.config != "large":
+        if rank == 0:
+            run_aux(args)
         return
 
     import torch

@@ -90,8 +90,9 @@ int sbg_limit_cpus(int n);
 int sbg_set_device_verbose(int on);
 int sbg_get_device_verbose(void);
 /* Engine knobs (0 = automatic): warps per CTA, rows per work item / 32,
- * variant (1 shared-memory, 2 global-memory, 3 shared-memory with a pointer
- * walk instead of index arithmetic), order (1 caller's, 2 sorted
+ * variant (1 shared-memory, 2 global-memory, 3 shared-memory with a two-load
+ * walk, 4 hybrid: columns in shared memory, rows read through L1), order
+ * (1 caller's, 2 sorted
  * by breakpoint count), output bytes per pipeline band. */
 int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes);
 
@@ -184,6 +185,37 @@ uint64_t sbg_enumerate_items(int skip_mode, uint64_t n_rows, uint64_t n_cols, ui
  * FP32 FFMA, 1 = FP64 DFMA, in lane-operations per second (one FMA
  * instruction per lane = one lane-op), from a register-only FMA loop. */
 int sbg_measure_peak(int kind, double* lane_ops_per_s);
+
+/* ---- batches: many independent problems in one persistent launch ----------------
+ * No single counterpart in the reference (it runs one problem per task); each
+ * problem is what create_cuda_block_integrate_{l1,lp,l2_kernel}_task computes.
+ * Plan once, launch many times.  Problems are device-resident pdist or kernel
+ * problems of one dtype and operation; their outputs are device buffers in
+ * DistanceMatrix / SymmetricMatrix order. */
+typedef struct sbg_problem {
+  const void* points;           /* device: interleaved (t, v) */
+  const uint64_t* offsets;      /* device: n + 1 offsets */
+  const uint64_t* host_offsets; /* optional host copy of offsets (NULL: read back once at create) */
+  uint64_t n;
+  void* out;                    /* device output, n(n-1)/2 or n(n+1)/2 elements */
+} sbg_problem;
+
+typedef struct sbg_batch sbg_batch;
+#define SBG_BATCH_GRAPH 1         /* launch through a captured CUDA graph */
+#define SBG_BATCH_CALLER_ORDER 2  /* keep the caller's PCF order (default: sorted by breakpoint count) */
+
+/* Builds the batch: length orders, packed layouts, descriptors ordered by
+ * estimated merge work (largest first).  Synchronises the device once. */
+int sbg_batch_create(int dtype, int op, double p, int skip_mode, const sbg_problem* problems, uint64_t n_problems,
+                     int flags, sbg_batch** batch);
+/* Computes every problem of the batch on `stream` (queue reset + one kernel;
+ * graph replay when created with SBG_BATCH_GRAPH). */
+int sbg_batch_launch(sbg_batch* batch, void* stream);
+/* Times (warps per CTA, rows per work item) settings on this batch, keeps the
+ * fastest; *best_ms receives its time per launch. */
+int sbg_batch_autotune(sbg_batch* batch, void* stream, double* best_ms);
+int sbg_batch_info(const sbg_batch* batch, uint64_t* items, uint64_t* pairs, int* warps, int* rows_per_item);
+void sbg_batch_destroy(sbg_batch* batch);
 
 /* ---- device entry that allocates nothing --------------------------------------
  * No counterpart in the reference; an addition of this library.

@@ -68,6 +68,11 @@ SIGNATURES = {
                                  _U64, _U64, _P]),
     "sbg_pairwise_device_noalloc": (_I, [_I, _I, _D, _I, _P, _P, _U64, _U64, _P, _P, _U64, _U64, _P, _P,
                                          ctypes.c_uint32, _P, _U64, _U64, _U64, _P]),
+    "sbg_batch_create": (_I, [_I, _I, _D, _I, _P, _U64, _I, ctypes.POINTER(_P)]),
+    "sbg_batch_launch": (_I, [_P, _P]),
+    "sbg_batch_autotune": (_I, [_P, _P, ctypes.POINTER(_D)]),
+    "sbg_batch_info": (_I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "sbg_batch_destroy": (None, [_P]),
     "sbg_output_count": (_U64, [_I, _U64, _U64]),
     "sbg_measure_peak": (_I, [_I, ctypes.POINTER(_D)]),
     "sbg_enumerate_items": (_U64, [_I, _U64, _U64, _U64, _U64, ctypes.c_uint32, _P, _U64]),

@@ -164,43 +164,59 @@ namespace sbg
     const int U = kernel_unroll();
     const size_t es = sizeof(Elem<T>);
     const size_t reserve = 2048;  // static shared memory + slack
+    const size_t usable = dev.smem_optin > reserve ? dev.smem_optin - reserve : 0;
     const uint32_t lmax_c = std::max<uint32_t>(cs.lmax, 1);
     const uint32_t lmax_r = std::max<uint32_t>(rs.lmax, 1);
     const uint32_t row_cap = lmax_r + lmax_c + (uint32_t)U + 1;
     auto smem_for = [&](int w) { return (size_t)32 * lmax_c * es + (size_t)w * row_cap * es; };
 
-    int variant = settings().variant.load();
-    int want_w = settings().warps.load();
+    const int variant = settings().variant.load();
+    const int want_w = settings().warps.load();
+    // Shared-memory variants (rows and columns staged): the most warps that fit.
     int warps = 0;
-    if (variant != 2)
+    if (variant == 0 || variant == 1 || variant == 3)
     {
-      // (variants 1 and 3 both stage in shared memory)
       const int cands[] = {32, 24, 16, 12, 8, 4};
       for (int w : cands)
       {
         if (want_w > 0 && w > want_w) continue;
-        if (smem_for(w) + reserve <= dev.smem_optin) { warps = w; break; }
+        if (smem_for(w) <= usable) { warps = w; break; }
       }
     }
     if ((variant == 1 || variant == 3) && warps == 0)
       throw Error(ST_INVALID_ARGUMENT, "shared-memory variant requested but the PCFs do not fit in shared memory");
-    if (warps > 0)
+
+    if ((variant == 0 && warps >= 16) || variant == 1 || variant == 3)
     {
       pl.smem = true;
+      pl.packed = false;
       pl.kvar = variant == 3 ? 1 : 2;
       pl.warps = warps;
       pl.lmax_c = lmax_c;
       pl.row_cap = row_cap;
       pl.smem_bytes = smem_for(warps);
     }
-    else
+    else if (variant == 2)
     {
       pl.smem = false;
+      pl.packed = true;
       pl.kvar = 0;
       pl.warps = want_w > 0 ? std::min(want_w, 32) : 16;
       pl.lmax_c = lmax_c;
       pl.row_cap = 0;
       pl.smem_bytes = 0;
+    }
+    else
+    {
+      // hybrid: columns staged when the group fits, rows through L1
+      pl.smem = true;
+      pl.packed = true;
+      pl.kvar = 3;
+      pl.warps = want_w > 0 ? std::min(want_w, 32) : 32;
+      const uint32_t cap = (uint32_t)std::min<size_t>(usable / (32 * es), 0xffffffffu);
+      pl.lmax_c = std::min(lmax_c, cap);
+      pl.row_cap = 0;
+      pl.smem_bytes = (size_t)32 * pl.lmax_c * es;
     }
 
     // Rows per item = 32 q: as large as possible (fewer column reloads,
@@ -216,7 +232,7 @@ namespace sbg
     }
     pl.q = q;
     const uint64_t items = items_for(mode, 0, nr, nc, q);
-    const int ctas_per_sm = pl.smem ? 1 : 2;
+    const int ctas_per_sm = (pl.kvar == 0) ? 2 : 1;
     pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(items, (uint64_t)dev.sms * ctas_per_sm));
     return pl;
   }
@@ -392,7 +408,7 @@ namespace sbg
     // Packed segment layout for the global-memory variant (needs the point
     // totals, read back with one synchronisation).
     std::unique_ptr<AsyncBuf<T>> rpack, cpack;
-    if (!pl.smem)
+    if (pl.packed)
     {
       uint64_t rtot = 0, ctot = 0;
       SBG_CUDA(cudaMemcpyAsync(&rtot, rows.off + rows.n, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
@@ -431,7 +447,7 @@ namespace sbg
     ls.lmax = lmax; ls.lmin = 1; ls.mean = lmax;
     const Plan pl = make_plan<T>(mode, n_rows, mode == MODE_CROSS ? n_cols : n_rows, ls, ls, dev);
     size_t need = 256;  // work-queue counter
-    if (!pl.smem)
+    if (pl.packed)
     {
       need += ((sizeof(Elem<T>) * row_points + 255) / 256) * 256;
       if (mode == MODE_CROSS) need += ((sizeof(Elem<T>) * col_points + 255) / 256) * 256;
@@ -473,7 +489,7 @@ namespace sbg
       d.out_count = hi > out_base ? hi - out_base : 0;
     }
     char* base = static_cast<char*>(scratch);
-    if (!pl.smem)
+    if (pl.packed)
     {
       Elem<T>* rp = reinterpret_cast<Elem<T>*>(base + 256);
       SBG_CUDA(launch_pack<T>(rows.pts, rows.off, rows.n, rp, row_points, dev.sms, st));
@@ -655,7 +671,7 @@ namespace sbg
     DeviceBuffer rpack, cpack;
     const T* kr_pts = drows.view.pts;
     const T* kc_pts = (mode == MODE_CROSS) ? dcols.view.pts : drows.view.pts;
-    if (!pl.smem)
+    if (pl.packed)
     {
       rpack.reset(sizeof(Elem<T>) * std::max<uint64_t>(1, rows.off[rows.n]));
       SBG_CUDA(launch_pack<T>(drows.view.pts, drows.view.off, rows.n, rpack.as<Elem<T>>(), rows.off[rows.n], dev.sms,

@@ -302,6 +302,166 @@ namespace sbg
     }
   }
 
+  // ---- hybrid variant: columns in shared memory, rows through L1 -------------
+  //
+  // Rows are read from the packed segment layout in global memory (all lanes
+  // of a warp read the same row at nearby positions, so the reads hit L1);
+  // the row index stops at the row's last element.  No per-warp row buffers:
+  // all shared memory holds columns, so longer PCFs fit and more warps run.
+  // A column group longer than the shared-memory block falls back to reading
+  // its columns from global memory too.
+
+  __device__ __forceinline__ void advance_hybrid(float& fv, float& ft, float& gv, float& gt, const Elem<float>* row,
+                                                 uint32_t& fi, uint32_t flast, uint32_t& ag)
+  {
+    asm("{\n\t.reg .pred p;\n\t.reg .u64 a;\n\t"
+        "setp.le.f32 p, %1, %3;\n\t"
+        "@p add.u32 %4, %4, 1;\n\t"
+        "min.u32 %4, %4, %7;\n\t"
+        "@!p add.u32 %5, %5, 256;\n\t"
+        "mad.wide.u32 a, %4, 8, %6;\n\t"
+        "@p ld.global.nc.v2.f32 {%0, %1}, [a];\n\t"
+        "@!p ld.shared.v2.f32 {%2, %3}, [%5];\n\t}"
+        : "+f"(fv), "+f"(ft), "+f"(gv), "+f"(gt), "+r"(fi), "+r"(ag)
+        : "l"(row), "r"(flast));
+  }
+
+  __device__ __forceinline__ void advance_hybrid(double& fv, double& ft, double& gv, double& gt,
+                                                 const Elem<double>* row, uint32_t& fi, uint32_t flast, uint32_t& ag)
+  {
+    asm("{\n\t.reg .pred p;\n\t.reg .u64 a;\n\t"
+        "setp.le.f64 p, %1, %3;\n\t"
+        "@p add.u32 %4, %4, 1;\n\t"
+        "min.u32 %4, %4, %7;\n\t"
+        "@!p add.u32 %5, %5, 512;\n\t"
+        "mad.wide.u32 a, %4, 16, %6;\n\t"
+        "@p ld.global.nc.v2.f64 {%0, %1}, [a];\n\t"
+        "@!p ld.shared.v2.f64 {%2, %3}, [%5];\n\t}"
+        : "+d"(fv), "+d"(ft), "+d"(gv), "+d"(gt), "+r"(fi), "+r"(ag)
+        : "l"(row), "r"(flast));
+  }
+
+  template <typename T, int K, int U>
+  __device__ __forceinline__ T merge_hybrid(const Elem<T>* row, uint32_t rlen, const Elem<T>* pg, uint32_t steps, T p)
+  {
+    Elem<T> F = row[0];
+    Elem<T> G = *pg;
+    uint32_t fi = 0;
+    const uint32_t flast = rlen - 1;
+    uint32_t ag = (uint32_t)__cvta_generic_to_shared(pg);
+    T t = T(0), acc = T(0), comp = T(0);
+    const uint32_t nblk = (steps + U - 1) / U;
+    for (uint32_t b = 0; b < nblk; ++b)
+    {
+      T blk = T(0);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+      {
+        const T tn = fmin(F.tn, G.tn);
+        blk += PairOp<K>::seg(tn - t, F.v, G.v, p);
+        t = tn;
+        advance_hybrid(F.v, F.tn, G.v, G.tn, row, fi, flast, ag);
+      }
+      kahan_add(acc, comp, blk);
+    }
+    return PairOp<K>::fin(acc - comp, p);
+  }
+
+  // Rows and columns come from the packed segment layout (rpts / cpts of the
+  // descriptors point at Elem<T> arrays at the CSR offsets).
+  template <typename T, int K, int U>
+  __global__ void __launch_bounds__(1024, 1) pairs_hybrid_kernel(const __grid_constant__ LaunchParams<T> L)
+  {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Elem<T>* cols = reinterpret_cast<Elem<T>*>(smem_raw);
+    __shared__ unsigned long long s_item;
+    __shared__ unsigned int s_next_row;
+
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+
+    for (;;)
+    {
+      if (threadIdx.x == 0)
+      {
+        s_item = atomicAdd(L.queue, 1ull);
+        s_next_row = 0;
+      }
+      __syncthreads();
+      const unsigned long long item = s_item;
+      if (item >= L.total_items) break;
+
+      const ProblemDesc<T>* Pp = L.probs ? L.probs + find_problem(L.probs, L.n_probs, item) : &L.one;
+      const int mode = Pp->mode;
+      const uint64_t nc = Pp->nc;
+      const uint64_t G = ceil_div_u64(nc, 32);
+      const uint64_t local = item - Pp->item_begin;
+      uint64_t c, g;
+      if (mode == MODE_CROSS) { c = local / G; g = local % G; }
+      else tri_decode(local, Pp->row_begin, Pp->row_end, Pp->q, G, &c, &g);
+      uint64_t row_lo = Pp->row_begin + c * 32ull * Pp->q;
+      uint64_t row_hi = row_lo + 32ull * Pp->q;
+      if (row_hi > Pp->row_end) row_hi = Pp->row_end;
+      const uint64_t col0 = 32ull * g;
+      if (mode != MODE_CROSS)
+      {
+        const uint64_t first = col0 + (mode == MODE_PDIST ? 1 : 0);
+        if (row_lo < first) row_lo = first;
+      }
+
+      const uint64_t cj = col0 + lane;
+      const bool cvalid = cj < nc;
+      const uint64_t cj_eff = cvalid ? cj : col0;
+      const uint64_t corig = Pp->cperm ? Pp->cperm[cj_eff] : cj_eff;
+      const uint64_t coff = Pp->coff[corig];
+      const uint32_t clen = (uint32_t)(Pp->coff[corig + 1] - coff);
+      const uint32_t maxlc = warp_max_u32(clen);
+      const T p = Pp->p;
+      const Elem<T>* ck = reinterpret_cast<const Elem<T>*>(Pp->cpts);
+      const Elem<T>* rk = reinterpret_cast<const Elem<T>*>(Pp->rpts);
+
+      const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > Pp->ccap);
+      const bool staged = item_ok && maxlc <= L.lmax_c;  // CTA-uniform
+      if (staged)
+      {
+        for (uint32_t k = warp; k < maxlc; k += nwarps)
+          if (k < clen) cols[(size_t)k * 32 + lane] = ck[coff + k];
+        __syncthreads();
+      }
+
+      if (item_ok)
+      {
+        for (;;)
+        {
+          unsigned r = 0;
+          if (lane == 0) r = atomicAdd(&s_next_row, 1u);
+          r = __shfl_sync(FULL, r, 0);
+          const uint64_t i = row_lo + r;
+          if (i >= row_hi) break;
+          const uint64_t iorig = Pp->rperm ? Pp->rperm[i] : i;
+          const uint64_t roff = Pp->roff[iorig];
+          const uint32_t rlen = (uint32_t)(Pp->roff[iorig + 1] - roff);
+          const bool ok = cvalid && (mode == MODE_CROSS || (mode == MODE_PDIST ? cj < i : cj <= i));
+          if (!__any_sync(FULL, ok) || rlen == 0 || roff + rlen > Pp->rcap) continue;
+          const uint32_t steps = rlen + maxlc - 1;
+          T res;
+          if (staged) res = merge_hybrid<T, K, U>(rk + roff, rlen, cols + lane, steps, p);
+          else res = merge_pair<T, K, U, 1, true>(rk + roff, ck + coff, steps, rlen, p);
+          if (ok)
+          {
+            uint64_t idx;
+            if (mode == MODE_CROSS) idx = iorig * Pp->ld + corig;
+            else idx = condensed_index(mode, iorig, corig);
+            const uint64_t rel = idx - Pp->out_base;
+            if (rel < Pp->out_count) Pp->out[rel] = res;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+
   // Segment layout in global memory: element k of PCF i (at the PCF's own
   // CSR offset) holds (v_k, t_{k+1}), the last one (v_{L-1}, TMAX).
   template <typename T>
@@ -351,12 +511,32 @@ namespace sbg
   }
 
   template <typename T>
+  static cudaError_t launch_hybrid(int opk, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const LaunchParams<T>& L)
+  {
+    constexpr int U = kUnrollConst;
+    void (*fn)(const LaunchParams<T>) = nullptr;
+    switch (opk)
+    {
+      case OPK_L1: fn = pairs_hybrid_kernel<T, OPK_L1, U>; break;
+      case OPK_L2DIST: fn = pairs_hybrid_kernel<T, OPK_L2DIST, U>; break;
+      case OPK_LP: fn = pairs_hybrid_kernel<T, OPK_LP, U>; break;
+      case OPK_INNER: fn = pairs_hybrid_kernel<T, OPK_INNER, U>; break;
+      default: return cudaErrorInvalidValue;
+    }
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, block, smem, s>>>(L);
+    return cudaGetLastError();
+  }
+
+  template <typename T>
   cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, int variant, int warps, int grid,
                            size_t smem_bytes, cudaStream_t s)
   {
     dim3 g((unsigned)grid), b((unsigned)(warps * 32));
     if (variant == 1) return launch_op<T, 1>(opk, g, b, smem_bytes, s, L);
     if (variant == 2) return launch_op<T, 2>(opk, g, b, smem_bytes, s, L);
+    if (variant == 3) return launch_hybrid<T>(opk, g, b, smem_bytes, s, L);
     return launch_op<T, 0>(opk, g, b, 0, s, L);
   }
 

@@ -65,7 +65,7 @@ namespace sbg
     // Engine knobs (0 = automatic).
     std::atomic<int> warps{0};
     std::atomic<int> rowChunk{0};        // Q: rows per work item = 32 * Q
-    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory, 2 global-memory, 3 shared-memory pointer walk
+    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory, 2 global-memory, 3 shared-memory pointer walk, 4 hybrid
     std::atomic<int> order{0};           // 0 auto, 1 caller order, 2 length-sorted
     std::atomic<uint64_t> bandBytes{0};  // output bytes per pipeline band (0 = auto)
     std::atomic<int> outputMode{0};      // host results: 0 auto (staged), 1 staged copy, 2 direct stores (coherent hosts)
@@ -125,7 +125,9 @@ namespace sbg
   struct Plan
   {
     bool smem = true;
-    int kvar = 2;      // kernel variant: 0 global memory, 1 shared two-load walk, 2 shared predicated walk
+    int kvar = 2;      // kernel variant: 0 global memory, 1 shared two-load walk, 2 shared predicated walk,
+                       // 3 hybrid (columns in shared memory, rows through L1)
+    bool packed = false;  // the kernel reads the packed segment layout (variants 0 and 3)
     int warps = 16;
     int grid = 1;
     uint32_t q = 1;

@@ -13,7 +13,8 @@ parity tests use:
                       reach 0 long before L for long PCFs; the generator
                       follows that recipe literally.
 * ``betti``         — integer values from a reflected walk v_k = |v_{k-1} + xi|,
-                      xi = +-1, v_0 ~ U{0..10}, last value 0, Exp(1) gaps.
+                      xi = +-1, v_0 ~ U{0..10}, last value 0, Exp(1) gaps
+                      (generated as |v_0 + xi_1 + ... + xi_k|, the same law).
 
 Times are generated in float64 and cast to the target type; a time that
 collides with its predecessor after the cast is moved up by one ulp, so every
@@ -97,16 +98,15 @@ def betti(n: int, lengths, dtype=np.float32, seed: int = 0):
     starts = np.zeros(n, dtype=np.int64)
     np.cumsum(lens[:-1], out=starts[1:])
     xi = rng.choice(np.array([-1.0, 1.0]), size=total)
-    v = np.empty(total, dtype=np.float64)
     v0 = rng.integers(0, 11, size=n).astype(np.float64)
-    # reflected walk, per PCF (sequential by nature)
-    for i in range(n):
-        a, b = starts[i], starts[i] + lens[i]
-        cur = v0[i]
-        v[a] = cur
-        for k in range(a + 1, b):
-            cur = abs(cur + xi[k])
-            v[k] = cur
+    xi[starts] = 0.0
+    # The reflected walk R_k = |R_{k-1} + xi_k| from an integer v_0 >= 0 is the
+    # Markov chain (0 -> 1; x -> x +- 1 with probability 1/2 each), which is
+    # exactly the law of |S_k| for the free walk S_k = v_0 + xi_1 + ... + xi_k;
+    # |S_k| is generated here without a per-point loop.
+    s = np.cumsum(xi)
+    s -= np.repeat(s[starts], lens)
+    v = np.abs(np.repeat(v0, lens) + s)
     v[_last_index(lens)] = 0.0
     return _pack(t, v.astype(dtype), lens, dtype)
 

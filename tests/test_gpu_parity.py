@@ -192,8 +192,14 @@ def test_variants_orders_and_bands_agree():
         srt = sb.pdist(X).data.copy()
         sb.set_tuning(variant=1, order=1, warps=4, row_chunk=1)
         small = sb.pdist(X).data.copy()
+        sb.set_tuning(variant=4, order=1)
+        hyb = sb.pdist(X).data.copy()
+        sb.set_tuning(variant=3, order=1)
+        two = sb.pdist(X).data.copy()
     finally:
         sb.set_tuning()
+    np.testing.assert_array_equal(hyb, base)
+    np.testing.assert_array_equal(two, base)
     np.testing.assert_array_equal(gm, base)
     np.testing.assert_array_equal(banded, base)
     np.testing.assert_array_equal(small, base)
