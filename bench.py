@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--cpu-sample-rows", type=int, default=0, help="rows in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="large", choices=["large", "plain", "stable_rank", "batched"],
+    ap.add_argument("--config", default="large", choices=["large", "plain", "stable_rank", "batched", "fwdbwd"],
                     help="large: the headline workload; the others print their own report line")
     return ap.parse_args()
 
@@ -166,6 +166,35 @@ def run_aux(args):
             b.close()
         rep.update({"workload": "512 problems, N_i~U{50..2000}, L~U{8..1024}, f32 Betti-like", "pairs": pairs,
                     "segments": segs})
+    elif args.config == "fwdbwd":
+        from stablebear_gb300 import autograd as ag
+        pts, off = synthetic.differentiation(4096, seed=0)
+        n = 4096
+        P = torch.tensor(pts, device="cuda", requires_grad=True)
+        O = torch.tensor(off.astype(np.int64), device="cuda")
+        G = torch.randn(n, n, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+        G = G + G.T
+        for name in ("l2_kernel", "l2"):
+            diag = name == "l2_kernel"
+
+            def fwd():
+                return ag.l2_kernel(P, O) if diag else ag.pdist(P, O, p=2)
+
+            def fwdbwd():
+                P.grad = None
+                M = fwd()
+                L = (G * ag.condensed_to_dense(M, n, diagonal=diag)).sum()
+                L.backward()
+
+            with torch.no_grad():
+                ms_f = _time_device(fwd, max(5, args.steps), 3)
+            ms_fb = _time_device(fwdbwd, max(5, args.steps), 3)
+            pairs = n * (n + 1) // 2 if diag else n * (n - 1) // 2
+            rep[name] = {"forward_ms": ms_f, "forward_pairs_per_s": pairs / (ms_f / 1e3),
+                         "fwd_bwd_ms": ms_fb, "fwd_bwd_pairs_per_s": pairs / (ms_fb / 1e3),
+                         "backward_over_forward": (ms_fb - ms_f) / ms_f}
+        rep.update({"workload": "N=4096 f32, L~U{16..512}, upstream G symmetric N(0,1); grads w.r.t. values and times",
+                    "segments_kernel": synthetic.segment_count(off, pts, 2)})
     print(json.dumps(rep), flush=True)
 
 

@@ -186,6 +186,21 @@ uint64_t sbg_enumerate_items(int skip_mode, uint64_t n_rows, uint64_t n_cols, ui
  * instruction per lane = one lane-op), from a register-only FMA loop. */
 int sbg_measure_peak(int kind, double* lane_ops_per_s);
 
+/* ---- gradients --------------------------------------------------------------------
+ * No counterpart in the reference (it has no gradients).  Given grad_out =
+ * dL/dM for the condensed output M of a pdist (L2: op SBG_OP_LP with p = 2, or
+ * L1) or L2 kernel problem, writes dL/d(points) into grad_points, laid out
+ * like the points: (n_points, 2) pairs [dL/dt, dL/dv].  forward_out is the
+ * forward result M (needed for the L2 distance, optional otherwise).  The
+ * merge is recomputed.  Times that coincide with a breakpoint of the other
+ * PCF of a pair (ties) and each PCF's first time t = 0 get no gradient from
+ * that pair.  Accumulation uses atomic adds (order not deterministic).
+ * Device pointers, stream-ordered; grad_points is overwritten. */
+int sbg_pairwise_backward_device(int dtype, int op, double p, int skip_mode,
+                                 const void* points, const uint64_t* offsets, uint64_t n, uint64_t n_points,
+                                 uint32_t max_points, const void* grad_out, const void* forward_out,
+                                 void* grad_points, void* stream);
+
 /* ---- batches: many independent problems in one persistent launch ----------------
  * No single counterpart in the reference (it runs one problem per task); each
  * problem is what create_cuda_block_integrate_{l1,lp,l2_kernel}_task computes.

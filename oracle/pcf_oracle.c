@@ -380,3 +380,117 @@ uint64_t sbo_count_total_segments(int dtype, int mode,
   }
   return total;
 }
+
+/* ---------------------------------------------------------------------- */
+/* FP64 reference gradient of  L = sum_pairs w_ij * M_ij  with respect to   */
+/* every breakpoint's value and time, for M = L2 kernel (op 2) or L2        */
+/* distance (op 1, p = 2).  The reference has no gradient; this is the      */
+/* analytic derivative of the rectangle sum of integrate()                  */
+/* (matrix_integrate.hpp:18-29), evaluated on the same rectangles:           */
+/*   d/dv (value of a rectangle's side) = (r - l) * d phi / d side value     */
+/*   d/dt_k (breakpoint k of one side, no tie) =                             */
+/*          phi(value before t_k) - phi(value after t_k)                     */
+/* with phi(f, g) = f g (kernel) or (f - g)^2 / (2 D) (distance, D the pair */
+/* distance; D = 0 gives no gradient).  Breakpoints that coincide with one   */
+/* of the other PCF (ties) get no time gradient.  Diagonal kernel entries:   */
+/* d/dv_k = 2 v_k (t_{k+1} - t_k), d/dt_k = v_{k-1}^2 - v_k^2.               */
+/* w: condensed weights in the output layout; grad: (M, 2) doubles           */
+/* [t-grad, v-grad], accumulated.  Single-threaded (small problems).         */
+/* ---------------------------------------------------------------------- */
+
+static void sbo_grad_pair_f64(const double* f, uint64_t lf, double* gf, const double* g, uint64_t lg, double* gg,
+                              int op, double w, double D, double bmax)
+{
+  if (w == 0.0) return;
+  double scale = w;
+  if (op == SBO_OP_LP) {
+    if (!(D > 0.0)) return;
+    scale = w / D;
+  }
+  size_t fi = 0, gi = 0;
+  double t = 0.0;
+  for (;;) {
+    int fn = fi + 1 < lf, gn = gi + 1 < lg;
+    double fv = f[2 * fi + 1], gv = g[2 * gi + 1];
+    double right;
+    int adv_f = 0, adv_g = 0;
+    if (fn && gn) {
+      double delta = f[2 * (fi + 1)] - g[2 * (gi + 1)];
+      if (delta <= 0) adv_f = 1;
+      if (delta >= 0) adv_g = 1;
+    } else if (fn) adv_f = 1;
+    else if (gn) adv_g = 1;
+    if (!adv_f && !adv_g) right = bmax;
+    else right = adv_f ? f[2 * (fi + 1)] : g[2 * (gi + 1)];
+    double dt = right - t;
+    /* value gradients of this rectangle */
+    if (op == SBO_OP_L2) {
+      gf[2 * fi + 1] += scale * dt * gv;
+      gg[2 * gi + 1] += scale * dt * fv;
+    } else if (op == SBO_OP_L1) {
+      double sg = fv > gv ? 1.0 : (fv < gv ? -1.0 : 0.0);
+      gf[2 * fi + 1] += scale * dt * sg;
+      gg[2 * gi + 1] -= scale * dt * sg;
+    } else {
+      gf[2 * fi + 1] += scale * dt * (fv - gv);
+      gg[2 * gi + 1] += scale * dt * (gv - fv);
+    }
+    if (!adv_f && !adv_g) break;
+    int tie = adv_f && adv_g;
+    if (adv_f) ++fi;
+    if (adv_g) ++gi;
+    if (!tie) {
+      if (adv_f) {
+        double a = f[2 * (fi - 1) + 1], b = f[2 * fi + 1];
+        double d = (op == SBO_OP_L2) ? (a - b) * gv
+                 : (op == SBO_OP_L1) ? fabs(a - gv) - fabs(b - gv)
+                 : 0.5 * ((a - gv) * (a - gv) - (b - gv) * (b - gv));
+        gf[2 * fi] += scale * d;
+      } else {
+        double a = g[2 * (gi - 1) + 1], b = g[2 * gi + 1];
+        double d = (op == SBO_OP_L2) ? (a - b) * fv
+                 : (op == SBO_OP_L1) ? fabs(a - fv) - fabs(b - fv)
+                 : 0.5 * ((a - fv) * (a - fv) - (b - fv) * (b - fv));
+        gg[2 * gi] += scale * d;
+      }
+    }
+    t = right;
+  }
+}
+
+static void sbo_grad_diag_f64(const double* f, uint64_t lf, double* gf, double w, double bmax)
+{
+  if (w == 0.0) return;
+  for (uint64_t k = 0; k < lf; ++k) {
+    double right = (k + 1 < lf) ? f[2 * (k + 1)] : bmax;
+    double v = f[2 * k + 1];
+    gf[2 * k + 1] += w * 2.0 * v * (right - f[2 * k]);
+    if (k > 0) {
+      double a = f[2 * (k - 1) + 1];
+      gf[2 * k] += w * (a * a - v * v);
+    }
+  }
+}
+
+/* pts: (M,2) doubles; mode 1 (distance: op LP means p = 2, op L1 the L1
+ * distance) or 2 (kernel, op L2). */
+int sbo_gradient_f64(const double* pts, const uint64_t* off, uint64_t n, int op, int mode, const double* w,
+                     const double* dist, double* grad, double bmax)
+{
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t jend = (mode == 1) ? i : i + 1;
+    for (uint64_t j = 0; j < jend; ++j) {
+      uint64_t idx = sbo_cond_index(mode, i, j);
+      const double* fp = pts + 2 * off[i];
+      const double* gp = pts + 2 * off[j];
+      uint64_t lf = off[i + 1] - off[i], lg = off[j + 1] - off[j];
+      if (i == j) {
+        sbo_grad_diag_f64(fp, lf, grad + 2 * off[i], w[idx], bmax);
+      } else {
+        sbo_grad_pair_f64(fp, lf, grad + 2 * off[i], gp, lg, grad + 2 * off[j], op, w[idx],
+                          dist ? dist[idx] : 0.0, bmax);
+      }
+    }
+  }
+  return 0;
+}

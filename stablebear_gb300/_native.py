@@ -68,6 +68,7 @@ SIGNATURES = {
                                  _U64, _U64, _P]),
     "sbg_pairwise_device_noalloc": (_I, [_I, _I, _D, _I, _P, _P, _U64, _U64, _P, _P, _U64, _U64, _P, _P,
                                          ctypes.c_uint32, _P, _U64, _U64, _U64, _P]),
+    "sbg_pairwise_backward_device": (_I, [_I, _I, _D, _I, _P, _P, _U64, _U64, ctypes.c_uint32, _P, _P, _P, _P]),
     "sbg_batch_create": (_I, [_I, _I, _D, _I, _P, _U64, _I, ctypes.POINTER(_P)]),
     "sbg_batch_launch": (_I, [_P, _P]),
     "sbg_batch_autotune": (_I, [_P, _P, ctypes.POINTER(_D)]),

@@ -1,0 +1,94 @@
+"""Differentiable pairwise integrals: a ``torch.autograd.Function`` whose
+forward is the pair kernel and whose backward is the hand-written backward
+kernel (``sbg_pairwise_backward_device``).
+
+The PCFs are a CUDA ``points`` tensor ``(M, 2)`` of ``(t, v)`` rows and an
+``offsets`` tensor ``(N + 1,)`` (the reference's CSR).  The result is the
+condensed matrix (``DistanceMatrix`` order for distances, ``SymmetricMatrix``
+order for the kernel); ``condensed_to_dense`` expands it.  Gradients flow to
+the values and to the breakpoint times (not to t = 0, and not at ties with a
+breakpoint of the other PCF of a pair).  torch is plumbing here: device
+memory and the autograd graph; both passes are native kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _native as nat
+
+_KINDS = {
+    "l2_kernel": (nat.OP_L2_INNER, 1.0, nat.SKIP_LOWER),
+    "l2": (nat.OP_LP, 2.0, nat.SKIP_LOWER_NODIAG),
+    "l1": (nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG),
+}
+
+
+def _code(t):
+    if t.dtype == torch.float32:
+        return nat.F32
+    if t.dtype == torch.float64:
+        return nat.F64
+    raise TypeError("points must be float32 or float64")
+
+
+def _stream(dev):
+    return ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+
+class PairwiseIntegral(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, points, offsets, kind, max_points):
+        op, p, skip = _KINDS[kind]
+        points = points.contiguous()
+        offsets = offsets.contiguous()
+        n = offsets.numel() - 1
+        count = int(nat.lib().sbg_output_count(skip, n, n))
+        out = torch.empty(count, dtype=points.dtype, device=points.device)
+        if count:
+            nat.check(nat.lib().sbg_pairwise_device(_code(points), op, p, skip, points.data_ptr(), offsets.data_ptr(),
+                                                    n, None, None, 0, None, None, int(max_points), out.data_ptr(), 0,
+                                                    0, 0, _stream(points.device)))
+        ctx.save_for_backward(points, offsets, out)
+        ctx.kind = kind
+        ctx.max_points = int(max_points)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        points, offsets, out = ctx.saved_tensors
+        op, p, skip = _KINDS[ctx.kind]
+        n = offsets.numel() - 1
+        grad = torch.empty_like(points)
+        go = grad_out.contiguous()
+        nat.check(nat.lib().sbg_pairwise_backward_device(_code(points), op, p, skip, points.data_ptr(),
+                                                         offsets.data_ptr(), n, points.shape[0], ctx.max_points,
+                                                         go.data_ptr(), out.data_ptr(), grad.data_ptr(),
+                                                         _stream(points.device)))
+        return grad, None, None, None
+
+
+def _max_points(offsets):
+    return int((offsets[1:] - offsets[:-1]).max().item()) if offsets.numel() > 1 else 1
+
+
+def l2_kernel(points, offsets):
+    """Condensed L2 Gram matrix (SymmetricMatrix order), differentiable."""
+    return PairwiseIntegral.apply(points, offsets, "l2_kernel", _max_points(offsets))
+
+
+def pdist(points, offsets, p=2):
+    """Condensed L1 or L2 distance matrix (DistanceMatrix order), differentiable."""
+    if p not in (1, 2):
+        raise ValueError("gradients are implemented for p = 1 and p = 2")
+    return PairwiseIntegral.apply(points, offsets, "l1" if p == 1 else "l2", _max_points(offsets))
+
+
+def condensed_to_dense(c, n, diagonal):
+    """Expand a condensed vector to the symmetric n x n matrix (differentiable)."""
+    k = 0 if diagonal else -1
+    r, s = torch.tril_indices(n, n, offset=k, device=c.device)
+    dense = torch.zeros(n, n, dtype=c.dtype, device=c.device)
+    dense = dense.index_put((r, s), c)
+    return dense + torch.tril(dense, -1).transpose(0, 1)

@@ -1,0 +1,323 @@
+// Backward pass of the pairwise integrals: given dL/dM for the condensed
+// output M (L2 kernel, L2 distance or L1 distance), accumulate dL/dv and
+// dL/dt for every breakpoint of every PCF.  The reference has no gradients;
+// this differentiates the rectangle sum of integrate()
+// (include/sbear/algorithms/functional/matrix_integrate.hpp:18-29) and
+// recomputes the merge instead of storing it.
+//
+// For one pair with weight w = dL/dM_ij and phi(f, g) the integrand
+// (f g, (f - g)^2, |f - g|):
+//   d/d(value of a rectangle's side) = w s (r - l) d phi / d side
+//   d/d t_k (a breakpoint of one side) = w s (phi(before t_k) - phi(after t_k))
+// with s = 1 (kernel, L1) or 1 / (2 D_ij) (L2 distance, from the forward
+// result; D = 0 contributes nothing).  A breakpoint that coincides with one of
+// the other PCF (a tie) has no derivative and gets no time gradient.  The
+// kernel's diagonal <f, f> is handled in closed form by diag_backward_kernel.
+//
+// Work decomposition: the forward kernel's items; a warp merges one row with
+// 32 columns.  Each lane keeps running sums for the row segment and the
+// column segment it is in and flushes a sum when its side advances: row
+// gradients go to a per-warp shared-memory buffer (flushed to global memory
+// once per row), column gradients straight to global memory.  Atomic adds:
+// the summation order is not deterministic.
+#include "../../include/sbgpu.h"
+#include "sbg_internal.hpp"
+
+#include <algorithm>
+#include <memory>
+
+namespace sbg
+{
+  enum BwdOp : int { BWD_INNER = 0, BWD_L2DIST = 1, BWD_L1DIST = 2 };
+
+  template <typename T>
+  struct BwdParams
+  {
+    const Elem<T>* pk;      // packed segment layout at the CSR offsets
+    const uint64_t* off;
+    uint64_t n;
+    uint64_t npts;
+    int mode;               // MODE_PDIST or MODE_KERNEL
+    uint32_t q;
+    uint64_t total_items;
+    unsigned long long* queue;
+    const T* grad_out;      // condensed dL/dM
+    const T* fwd;           // condensed M (distances), or null
+    T* grad;                // (npts, 2): [dL/dt, dL/dv]
+    uint32_t row_cap;       // per-warp shared gradient buffer (elements)
+  };
+
+  namespace
+  {
+    template <int OP, typename T>
+    __device__ __forceinline__ void seg_coeffs(T f, T g, T& cf, T& cg)
+    {
+      if (OP == BWD_INNER) { cf = g; cg = f; }
+      else if (OP == BWD_L2DIST) { cf = f - g; cg = g - f; }
+      else
+      {
+        const T d = f - g;
+        cf = d > T(0) ? T(1) : (d < T(0) ? T(-1) : T(0));
+        cg = -cf;
+      }
+    }
+
+    // phi(a, o) - phi(b, o): the change of the integrand when one side's value
+    // steps from a to b (at that side's breakpoint), the other side being o.
+    template <int OP, typename T>
+    __device__ __forceinline__ T step_delta(T a, T b, T o)
+    {
+      if (OP == BWD_INNER) return (a - b) * o;
+      if (OP == BWD_L2DIST) return T(0.5) * ((a - o) * (a - o) - (b - o) * (b - o));
+      return fabs(a - o) - fabs(b - o);
+    }
+  }
+
+  template <typename T, int OP>
+  __global__ void __launch_bounds__(512) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
+  {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sgrad_all = reinterpret_cast<T*>(smem_raw);
+    __shared__ unsigned long long s_item;
+    __shared__ unsigned int s_next_row;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    T* sg = sgrad_all + (size_t)warp * B.row_cap * 2;  // [k][2]: t-grad, v-grad
+    const unsigned FULL = 0xffffffffu;
+
+    for (;;)
+    {
+      if (threadIdx.x == 0)
+      {
+        s_item = atomicAdd(B.queue, 1ull);
+        s_next_row = 0;
+      }
+      __syncthreads();
+      const unsigned long long item = s_item;
+      if (item >= B.total_items) break;
+      const uint64_t G = ceil_div_u64(B.n, 32);
+      uint64_t c, g;
+      tri_decode(item, 0, B.n, B.q, G, &c, &g);
+      uint64_t row_lo = c * 32ull * B.q;
+      uint64_t row_hi = row_lo + 32ull * B.q;
+      if (row_hi > B.n) row_hi = B.n;
+      const uint64_t col0 = 32ull * g;
+      if (row_lo < col0 + 1) row_lo = col0 + 1;  // the diagonal is not handled here
+
+      const uint64_t cj = col0 + lane;
+      const bool cvalid = cj < B.n;
+      const uint64_t cj_eff = cvalid ? cj : col0;
+      const uint64_t coff = B.off[cj_eff];
+      const uint32_t clen = (uint32_t)(B.off[cj_eff + 1] - coff);
+      const uint32_t maxlc = __reduce_max_sync(FULL, clen);
+      const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > B.npts);
+
+      if (item_ok)
+      {
+        for (;;)
+        {
+          unsigned r = 0;
+          if (lane == 0) r = atomicAdd(&s_next_row, 1u);
+          r = __shfl_sync(FULL, r, 0);
+          const uint64_t i = row_lo + r;
+          if (i >= row_hi) break;
+          const uint64_t roff = B.off[i];
+          const uint32_t rlen = (uint32_t)(B.off[i + 1] - roff);
+          if (rlen == 0 || rlen > B.row_cap || roff + rlen > B.npts) continue;
+          const bool ok = cvalid && cj < i;
+          T w = T(0);
+          if (ok)
+          {
+            const uint64_t idx = condensed_index(B.mode, i, cj);
+            w = B.grad_out[idx];
+            if (OP == BWD_L2DIST)
+            {
+              const T D = B.fwd[idx];
+              w = D > T(0) ? w / D : T(0);
+            }
+          }
+          if (!__any_sync(FULL, w != T(0))) continue;
+
+          for (uint32_t k = lane; k < rlen; k += 32) { sg[2 * k] = T(0); sg[2 * k + 1] = T(0); }
+          __syncwarp();
+
+          const Elem<T>* row = B.pk + roff;
+          const Elem<T>* col = B.pk + coff;
+          Elem<T> F = row[0], Gc = col[0];
+          uint32_t fi = 0, gi = 0;
+          T t = T(0), accF = T(0), accG = T(0);
+          const uint32_t steps = rlen + maxlc - 1;
+          for (uint32_t s = 0; s < steps; ++s)
+          {
+            const bool takeF = row_first(F.tn, Gc.tn);
+            const T tn = takeF ? F.tn : Gc.tn;
+            const T dt = tn - t;
+            T cf, cg;
+            seg_coeffs<OP>(F.v, Gc.v, cf, cg);
+            accF = fma(dt, cf, accF);
+            accG = fma(dt, cg, accG);
+            if (takeF)
+            {
+              if (fi + 1 < rlen)
+              {
+                if (w != T(0)) atomicAdd(&sg[2 * fi + 1], w * accF);
+                accF = T(0);
+                const Elem<T> Fn = row[fi + 1];
+                if (w != T(0) && !(F.tn == Gc.tn)) atomicAdd(&sg[2 * (fi + 1)], w * step_delta<OP>(F.v, Fn.v, Gc.v));
+                ++fi;
+                F = Fn;
+              }
+            }
+            else
+            {
+              // Gc.tn < F.tn <= TMAX, so the column has a next element
+              if (w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
+              accG = T(0);
+              const Elem<T> Gn = col[gi + 1];
+              if (w != T(0) && !(Gc.tn == t)) atomicAdd(&B.grad[2 * (coff + gi + 1)], w * step_delta<OP>(Gc.v, Gn.v, F.v));
+              ++gi;
+              Gc = Gn;
+            }
+            t = tn;
+          }
+          if (w != T(0)) atomicAdd(&sg[2 * fi + 1], w * accF);
+          if (w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
+          __syncwarp();
+          for (uint32_t k = lane; k < rlen; k += 32)
+          {
+            const T gt = sg[2 * k], gv = sg[2 * k + 1];
+            if (gt != T(0)) atomicAdd(&B.grad[2 * (roff + k)], gt);
+            if (gv != T(0)) atomicAdd(&B.grad[2 * (roff + k) + 1], gv);
+          }
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // <f, f> = sum_k v_k^2 (t_{k+1} - t_k):  d/dv_k = 2 v_k (t_{k+1} - t_k),
+  // d/dt_k = v_{k-1}^2 - v_k^2, weighted by dL/dK_ii.  One warp per PCF.
+  template <typename T>
+  __global__ void diag_backward_kernel(const Elem<T>* __restrict__ pk, const uint64_t* __restrict__ off, uint64_t n,
+                                       uint64_t npts, const T* __restrict__ grad_out, T* __restrict__ grad)
+  {
+    const uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+    for (uint64_t i = wid; i < n; i += nw)
+    {
+      const uint64_t o = off[i], len = off[i + 1] - o;
+      if (len == 0 || o + len > npts) continue;
+      const T w = grad_out[i * (i + 1) / 2 + i];
+      if (w == T(0)) continue;
+      for (uint64_t k = lane; k < len; k += 32)
+      {
+        const Elem<T> e = pk[o + k];
+        const T tk = (k == 0) ? T(0) : pk[o + k - 1].tn;
+        grad[2 * (o + k) + 1] += w * T(2) * e.v * (e.tn - tk);
+        if (k > 0)
+        {
+          const T a = pk[o + k - 1].v;
+          grad[2 * (o + k)] += w * (a * a - e.v * e.v);
+        }
+      }
+    }
+  }
+
+  template <typename T>
+  static void backward_device(int op, double p, int mode, const T* pts, const uint64_t* off, uint64_t n,
+                              uint64_t npts, uint32_t lmax, const T* grad_out, const T* fwd, T* grad, cudaStream_t st)
+  {
+    int bop;
+    if (mode == MODE_KERNEL && op == SBG_OP_L2_INNER) bop = BWD_INNER;
+    else if (mode == MODE_PDIST && op == SBG_OP_LP && p == 2.0) bop = BWD_L2DIST;
+    else if (mode == MODE_PDIST && (op == SBG_OP_L1 || (op == SBG_OP_LP && p == 1.0))) bop = BWD_L1DIST;
+    else throw Error(ST_INVALID_ARGUMENT, "gradients exist for the L2 kernel (SBG_SKIP_LOWER), and L2 or L1 pdist");
+    if (bop == BWD_L2DIST && !fwd) throw Error(ST_INVALID_ARGUMENT, "the L2-distance gradient needs the forward result");
+    if (lmax == 0) throw Error(ST_INVALID_ARGUMENT, "max_points must be given");
+    const DeviceInfo dev = device_info();
+    SBG_CUDA(cudaMemsetAsync(grad, 0, sizeof(T) * 2 * npts, st));
+    if (n == 0) return;
+
+    void* packed = nullptr;
+    void* queue = nullptr;
+    SBG_CUDA(cudaMallocAsync(&packed, std::max<uint64_t>(1, npts) * sizeof(Elem<T>), st));
+    SBG_CUDA(cudaMallocAsync(&queue, 256, st));
+    struct Free
+    {
+      void* a; void* b; cudaStream_t s;
+      ~Free() { cudaFreeAsync(a, s); cudaFreeAsync(b, s); }
+    } guard{packed, queue, st};
+    SBG_CUDA(launch_pack<T>(pts, off, n, static_cast<Elem<T>*>(packed), npts, dev.sms, st));
+
+    BwdParams<T> B{};
+    B.pk = static_cast<const Elem<T>*>(packed);
+    B.off = off; B.n = n; B.npts = npts; B.mode = mode;
+    B.grad_out = grad_out; B.fwd = fwd; B.grad = grad;
+    B.queue = static_cast<unsigned long long*>(queue);
+    B.row_cap = lmax;
+    const int warps = 16;
+    const size_t smem = (size_t)warps * lmax * 2 * sizeof(T);
+    if (smem + 2048 > dev.smem_optin) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
+    uint32_t q = 1;
+    for (uint32_t cand = 8; cand >= 1; cand /= 2)
+      if (tri_item_count(0, n, cand, ceil_div_u64(n, 32)) >= (uint64_t)dev.sms * 6) { q = cand; break; }
+    B.q = q;
+    B.total_items = tri_item_count(0, n, q, ceil_div_u64(n, 32));
+    SBG_CUDA(cudaMemsetAsync(queue, 0, 8, st));
+    if (B.total_items > 0)
+    {
+      void (*fn)(const BwdParams<T>) = bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER>
+                                     : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST>
+                                                         : pairs_backward_kernel<T, BWD_L1DIST>;
+      SBG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms);
+      fn<<<grid, warps * 32, smem, st>>>(B);
+      SBG_CUDA(cudaGetLastError());
+    }
+    if (bop == BWD_INNER)
+    {
+      // after the pair kernel on the same stream: plain adds are race-free
+      const unsigned blocks = (unsigned)std::min<uint64_t>((n + 7) / 8, (uint64_t)dev.sms * 8);
+      diag_backward_kernel<T><<<blocks, 256, 0, st>>>(B.pk, off, n, npts, grad_out, grad);
+      SBG_CUDA(cudaGetLastError());
+    }
+  }
+}
+
+extern "C" int sbg_pairwise_backward_device(int dtype, int op, double p, int skip_mode, const void* points,
+                                            const uint64_t* offsets, uint64_t n, uint64_t n_points,
+                                            uint32_t max_points, const void* grad_out, const void* forward_out,
+                                            void* grad_points, void* stream)
+{
+  using namespace sbg;
+  try
+  {
+    if (dtype != SBG_F32 && dtype != SBG_F64) throw Error(ST_INVALID_ARGUMENT, "dtype must be SBG_F32 or SBG_F64");
+    if (skip_mode != SBG_SKIP_LOWER && skip_mode != SBG_SKIP_LOWER_NODIAG)
+      throw Error(ST_INVALID_ARGUMENT, "gradients are defined for pdist and l2 kernel outputs");
+    if (n > 0 && (!points || !offsets || !grad_out || !grad_points)) throw Error(ST_INVALID_ARGUMENT, "null pointer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (dtype == SBG_F32)
+      backward_device<float>(op, p, skip_mode, static_cast<const float*>(points), offsets, n, n_points, max_points,
+                             static_cast<const float*>(grad_out), static_cast<const float*>(forward_out),
+                             static_cast<float*>(grad_points), st);
+    else
+      backward_device<double>(op, p, skip_mode, static_cast<const double*>(points), offsets, n, n_points, max_points,
+                              static_cast<const double*>(grad_out), static_cast<const double*>(forward_out),
+                              static_cast<double*>(grad_points), st);
+    set_last_error("");
+    return SBG_OK;
+  }
+  catch (const Error& e)
+  {
+    set_last_error(e.what());
+    return e.status;
+  }
+  catch (const std::exception& e)
+  {
+    set_last_error(e.what());
+    return SBG_ERR_INTERNAL;
+  }
+}

@@ -161,7 +161,7 @@ namespace sbg
   Plan make_plan(int mode, uint64_t nr, uint64_t nc, const LengthStats& rs, const LengthStats& cs, const DeviceInfo& dev)
   {
     Plan pl;
-    const int U = kernel_unroll();
+    const int U = kernel_unroll(sizeof(T) == 8);
     const size_t es = sizeof(Elem<T>);
     const size_t reserve = 2048;  // static shared memory + slack
     const size_t usable = dev.smem_optin > reserve ? dev.smem_optin - reserve : 0;

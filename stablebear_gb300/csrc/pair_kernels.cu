@@ -7,7 +7,13 @@
 
 namespace sbg
 {
-  constexpr int kUnrollConst = 8;  // rectangles per naive block sum (Kahan across blocks)
+  // Rectangles per naive block sum (blocks are combined with Kahan
+  // compensation): 8 for float; 16 for double, where the compensation's four
+  // FP64 adds cost more than a longer naive block loses (f64 sums of 16 terms
+  // stay far below the 1e-12 target).
+  template <typename T> struct Unroll;
+  template <> struct Unroll<float> { static constexpr int value = 8; };
+  template <> struct Unroll<double> { static constexpr int value = 16; };
 
   namespace
   {
@@ -73,9 +79,9 @@ namespace sbg
 #pragma unroll
       for (int u = 0; u < U; ++u)
       {
-        const bool takeF = F.tn <= G.tn;
+        const bool takeF = row_first(F.tn, G.tn);
         const T tn = takeF ? F.tn : G.tn;
-        blk += PairOp<K>::seg(tn - t, F.v, G.v, p);
+        blk = PairOp<K>::acc(blk, tn - t, F.v, G.v, p);
         t = tn;
         if (FCLAMP)
         {
@@ -117,8 +123,10 @@ namespace sbg
   __device__ __forceinline__ void advance_shared(double& fv, double& ft, double& gv, double& gt, uint32_t& af,
                                                  uint32_t& ag)
   {
-    asm("{\n\t.reg .pred p;\n\t"
-        "setp.le.f64 p, %1, %3;\n\t"
+    asm("{\n\t.reg .pred p;\n\t.reg .s64 fa, ga;\n\t"
+        "mov.b64 fa, %1;\n\t"
+        "mov.b64 ga, %3;\n\t"
+        "setp.le.s64 p, fa, ga;\n\t"
         "@p add.u32 %4, %4, 16;\n\t"
         "@!p add.u32 %5, %5, 512;\n\t"
         "@p ld.shared.v2.f64 {%0, %1}, [%4];\n\t"
@@ -143,8 +151,8 @@ namespace sbg
 #pragma unroll
       for (int u = 0; u < U; ++u)
       {
-        const T tn = fmin(F.tn, G.tn);
-        blk += PairOp<K>::seg(tn - t, F.v, G.v, p);
+        const T tn = earlier(F.tn, G.tn);
+        blk = PairOp<K>::acc(blk, tn - t, F.v, G.v, p);
         t = tn;
         advance_shared(F.v, F.tn, G.v, G.tn, af, ag);
       }
@@ -329,8 +337,10 @@ namespace sbg
   __device__ __forceinline__ void advance_hybrid(double& fv, double& ft, double& gv, double& gt,
                                                  const Elem<double>* row, uint32_t& fi, uint32_t flast, uint32_t& ag)
   {
-    asm("{\n\t.reg .pred p;\n\t.reg .u64 a;\n\t"
-        "setp.le.f64 p, %1, %3;\n\t"
+    asm("{\n\t.reg .pred p;\n\t.reg .u64 a;\n\t.reg .s64 fa, ga;\n\t"
+        "mov.b64 fa, %1;\n\t"
+        "mov.b64 ga, %3;\n\t"
+        "setp.le.s64 p, fa, ga;\n\t"
         "@p add.u32 %4, %4, 1;\n\t"
         "min.u32 %4, %4, %7;\n\t"
         "@!p add.u32 %5, %5, 512;\n\t"
@@ -357,8 +367,8 @@ namespace sbg
 #pragma unroll
       for (int u = 0; u < U; ++u)
       {
-        const T tn = fmin(F.tn, G.tn);
-        blk += PairOp<K>::seg(tn - t, F.v, G.v, p);
+        const T tn = earlier(F.tn, G.tn);
+        blk = PairOp<K>::acc(blk, tn - t, F.v, G.v, p);
         t = tn;
         advance_hybrid(F.v, F.tn, G.v, G.tn, row, fi, flast, ag);
       }
@@ -491,7 +501,7 @@ namespace sbg
   template <typename T, int VAR>
   static cudaError_t launch_op(int opk, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const LaunchParams<T>& L)
   {
-    constexpr int U = kUnrollConst;
+    constexpr int U = Unroll<T>::value;
     void (*fn)(const LaunchParams<T>) = nullptr;
     switch (opk)
     {
@@ -513,7 +523,7 @@ namespace sbg
   template <typename T>
   static cudaError_t launch_hybrid(int opk, dim3 grid, dim3 block, size_t smem, cudaStream_t s, const LaunchParams<T>& L)
   {
-    constexpr int U = kUnrollConst;
+    constexpr int U = Unroll<T>::value;
     void (*fn)(const LaunchParams<T>) = nullptr;
     switch (opk)
     {
@@ -559,5 +569,5 @@ namespace sbg
   template cudaError_t launch_pack<double>(const double*, const uint64_t*, uint64_t, Elem<double>*, uint64_t, int,
                                            cudaStream_t);
 
-  int kernel_unroll() { return kUnrollConst; }
+  int kernel_unroll(bool f64) { return f64 ? Unroll<double>::value : Unroll<float>::value; }
 }

@@ -57,10 +57,17 @@ namespace sbg
 
   template <int K> struct PairOp;
 
+  // acc(blk, dt, f, g) = blk + dt * op(f, g), with dt * op folded into one
+  // fused multiply-add (one rounding fewer than the reference's separate
+  // product and sum; the sum is compensated anyway).
   template <> struct PairOp<OPK_L1>
   {
     // |dt * (f - g)| == dt * |f - g| bit for bit, since dt >= 0.
     template <typename T> __device__ static __forceinline__ T seg(T dt, T f, T g, T) { return fabs(dt * (f - g)); }
+    template <typename T> __device__ static __forceinline__ T acc(T blk, T dt, T f, T g, T)
+    {
+      return fma(fabs(f - g), dt, blk);
+    }
     template <typename T> __device__ static __forceinline__ T fin(T x, T) { return x; }
   };
 
@@ -73,20 +80,50 @@ namespace sbg
       T d = f - g;
       return dt * (d * d);
     }
+    template <typename T> __device__ static __forceinline__ T acc(T blk, T dt, T f, T g, T)
+    {
+      const T d = f - g;
+      return fma(d * d, dt, blk);
+    }
     template <typename T> __device__ static __forceinline__ T fin(T x, T) { return sqrt(x); }
   };
 
   template <> struct PairOp<OPK_LP>
   {
     template <typename T> __device__ static __forceinline__ T seg(T dt, T f, T g, T p) { return dt * pow(fabs(f - g), p); }
+    template <typename T> __device__ static __forceinline__ T acc(T blk, T dt, T f, T g, T p)
+    {
+      return fma(pow(fabs(f - g), p), dt, blk);
+    }
     template <typename T> __device__ static __forceinline__ T fin(T x, T p) { return pow(x, T(1) / p); }
   };
 
   template <> struct PairOp<OPK_INNER>
   {
     template <typename T> __device__ static __forceinline__ T seg(T dt, T f, T g, T) { return dt * (f * g); }
+    template <typename T> __device__ static __forceinline__ T acc(T blk, T dt, T f, T g, T)
+    {
+      return fma(f * g, dt, blk);
+    }
     template <typename T> __device__ static __forceinline__ T fin(T x, T) { return x; }
   };
+
+  // The earlier of two breakpoint times.  float: one FMNMX.  double: the
+  // times are >= 0 (or clamped to TMAX), where the IEEE order equals the
+  // order of the bit patterns as signed 64-bit integers, so the compare and
+  // select run on the integer pipe instead of the (much narrower) FP64 pipe.
+  __device__ __forceinline__ float earlier(float a, float b) { return fminf(a, b); }
+  __device__ __forceinline__ double earlier(double a, double b)
+  {
+    return (__double_as_longlong(a) <= __double_as_longlong(b)) ? a : b;
+  }
+  // Whether the row side advances (its next time is not later; ties go to
+  // the row), with the same integer-order trick for double.
+  __device__ __forceinline__ bool row_first(float a, float b) { return a <= b; }
+  __device__ __forceinline__ bool row_first(double a, double b)
+  {
+    return __double_as_longlong(a) <= __double_as_longlong(b);
+  }
 
   // ---- problem descriptors ----------------------------------------------
 

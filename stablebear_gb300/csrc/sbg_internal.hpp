@@ -157,7 +157,7 @@ namespace sbg
   template <typename T>
   cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, uint64_t cap, int sms,
                           cudaStream_t s);
-  int kernel_unroll();
+  int kernel_unroll(bool f64);
 
   // Control block of one host-side run (progress, cancellation).
   struct RunControl

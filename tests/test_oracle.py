@@ -151,3 +151,51 @@ def test_oracle_matches_live_reference(dt):
         if True:
             np.testing.assert_array_equal(orc.evaluate(pts, off, op=op, p=p, mode=mode),
                                           orc.ref_evaluate(pts, off, op=op, p=p, mode=mode))
+
+
+def oracle_gradient(pts, off, op, mode, w, dist=None):
+    import ctypes
+    lib = orc._load()
+    lib.sbo_gradient_f64.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_uint64, ctypes.c_int, ctypes.c_int,
+                                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                              ctypes.c_double]
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    off = np.ascontiguousarray(off, dtype=np.uint64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    g = np.zeros_like(pts)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    d = np.ascontiguousarray(dist, dtype=np.float64) if dist is not None else None
+    lib.sbo_gradient_f64(P(pts), P(off), len(off) - 1, op, mode, P(w), P(d) if d is not None else None, P(g),
+                         float(np.finfo(np.float64).max))
+    return g
+
+
+@pytest.mark.parametrize("op,mode,p", [(orc.OP_L2, orc.MODE_KERNEL, 1.0), (orc.OP_LP, orc.MODE_PDIST, 2.0),
+                                       (orc.OP_L1, orc.MODE_PDIST, 1.0)])
+def test_oracle_gradient_matches_central_differences(op, mode, p):
+    """The FP64 reference gradient against FP64 central finite differences
+    of the double-double forward.  Excluded: t_0 (fixed at 0) and each PCF's
+    last value, whose rectangle runs to numeric_limits<double>::max()."""
+    from stablebear_gb300 import synthetic
+    pts, off = synthetic.gaussian(8, synthetic.uniform_lengths(3, 9), np.float64, seed=3)
+    M = orc.evaluate(pts, off, op=op, p=p, mode=mode, truth=True)
+    w = np.random.default_rng(1).standard_normal(M.size)
+    g = oracle_gradient(pts, off, op, mode, w, M if op == orc.OP_LP else None)
+    loss = lambda q: float(w @ orc.evaluate(q, off, op=op, p=p, mode=mode, truth=True))
+    starts = set(int(x) for x in off[:-1])
+    lasts = set(int(x) - 1 for x in off[1:])
+    eps = 1e-6
+    checked = 0
+    for k in range(len(pts)):
+        for c in (0, 1):
+            if (c == 0 and k in starts) or (c == 1 and k in lasts):
+                continue
+            q = pts.copy()
+            q[k, c] += eps
+            a = loss(q)
+            q[k, c] -= 2 * eps
+            b = loss(q)
+            fd = (a - b) / (2 * eps)
+            assert abs(fd - g[k, c]) <= 1e-6 * max(1.0, abs(fd)), (k, c, fd, g[k, c])
+            checked += 1
+    assert checked > 40
