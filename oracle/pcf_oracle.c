@@ -424,16 +424,18 @@ static void sbo_grad_pair_f64(const double* f, uint64_t lf, double* gf, const do
     else right = adv_f ? f[2 * (fi + 1)] : g[2 * (gi + 1)];
     double dt = right - t;
     /* value gradients of this rectangle */
+    /* dt * coefficient first: the last rectangle's dt is the type's max and
+       its coefficient usually 0 */
     if (op == SBO_OP_L2) {
-      gf[2 * fi + 1] += scale * dt * gv;
-      gg[2 * gi + 1] += scale * dt * fv;
+      gf[2 * fi + 1] += scale * (dt * gv);
+      gg[2 * gi + 1] += scale * (dt * fv);
     } else if (op == SBO_OP_L1) {
       double sg = fv > gv ? 1.0 : (fv < gv ? -1.0 : 0.0);
-      gf[2 * fi + 1] += scale * dt * sg;
-      gg[2 * gi + 1] -= scale * dt * sg;
+      gf[2 * fi + 1] += scale * (dt * sg);
+      gg[2 * gi + 1] -= scale * (dt * sg);
     } else {
-      gf[2 * fi + 1] += scale * dt * (fv - gv);
-      gg[2 * gi + 1] += scale * dt * (gv - fv);
+      gf[2 * fi + 1] += scale * (dt * (fv - gv));
+      gg[2 * gi + 1] += scale * (dt * (gv - fv));
     }
     if (!adv_f && !adv_g) break;
     int tie = adv_f && adv_g;
@@ -464,7 +466,7 @@ static void sbo_grad_diag_f64(const double* f, uint64_t lf, double* gf, double w
   for (uint64_t k = 0; k < lf; ++k) {
     double right = (k + 1 < lf) ? f[2 * (k + 1)] : bmax;
     double v = f[2 * k + 1];
-    gf[2 * k + 1] += w * 2.0 * v * (right - f[2 * k]);
+    gf[2 * k + 1] += w * (2.0 * (v * (right - f[2 * k])));
     if (k > 0) {
       double a = f[2 * (k - 1) + 1];
       gf[2 * k] += w * (a * a - v * v);
