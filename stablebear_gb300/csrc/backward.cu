@@ -18,10 +18,11 @@
 // 32 columns.  Each lane keeps running sums for the row segment and the
 // column segment it is in and flushes a sum when its side advances: row
 // gradients go to a per-warp shared-memory buffer (flushed to global memory
-// once per row), column gradients to a per-CTA shared-memory block shared by
-// all warps of the item (flushed once per item; straight to global memory
-// when the block does not fit).  Atomic adds: the summation order is not
-// deterministic.
+// once per row), column gradients straight to global memory.  (A per-CTA
+// shared block for the column gradients measured slower on GB300: the warps
+// of an item walk the same columns at similar speed and contend on the same
+// shared slots, while global atomics spread over the L2 slices.)  Atomic
+// adds: the summation order is not deterministic.
 #include "../../include/sbgpu.h"
 #include "sbg_internal.hpp"
 
@@ -47,8 +48,6 @@ namespace sbg
     const T* fwd;           // condensed M (distances), or null
     T* grad;                // (npts, 2): [dL/dt, dL/dv]
     uint32_t row_cap;       // per-warp shared gradient buffer (elements)
-    uint32_t col_cap;       // column gradients accumulate in shared memory for groups up to this
-                            // length (0: straight to global memory)
   };
 
   namespace
@@ -81,13 +80,11 @@ namespace sbg
   __global__ void __launch_bounds__(512) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
   {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* cgrad = reinterpret_cast<T*>(smem_raw);               // [k][32 lanes][2]
-    T* sgrad_all = cgrad + (size_t)B.col_cap * 32 * 2;        // per warp [k][2]
+    T* sgrad_all = reinterpret_cast<T*>(smem_raw);
     __shared__ unsigned long long s_item;
     __shared__ unsigned int s_next_row;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int nthreads = blockDim.x;
     T* sg = sgrad_all + (size_t)warp * B.row_cap * 2;  // [k][2]: t-grad, v-grad
     const unsigned FULL = 0xffffffffu;
 
@@ -117,18 +114,6 @@ namespace sbg
       const uint32_t clen = (uint32_t)(B.off[cj_eff + 1] - coff);
       const uint32_t maxlc = __reduce_max_sync(FULL, clen);
       const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > B.npts);
-      // Column gradients of this item: shared-memory block when the group
-      // fits (CTA-uniform), else global atomics.
-      const bool cshared = item_ok && maxlc <= B.col_cap;
-      if (cshared)
-      {
-        for (uint32_t e = threadIdx.x; e < maxlc * 64u; e += nthreads) cgrad[e] = T(0);
-        __syncthreads();
-      }
-      // gradient slot (t at [0], v at [1]) of this lane's column element k
-      auto cslot = [&](uint32_t k) -> T* {
-        return cshared ? cgrad + ((size_t)k * 32 + lane) * 2 : B.grad + 2 * (coff + k);
-      };
 
       if (item_ok)
       {
@@ -189,17 +174,17 @@ namespace sbg
             else
             {
               // Gc.tn < F.tn <= TMAX, so the column has a next element
-              if (w != T(0)) atomicAdd(cslot(gi) + 1, w * accG);
+              if (w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
               accG = T(0);
               const Elem<T> Gn = col[gi + 1];
-              if (w != T(0) && !(Gc.tn == t)) atomicAdd(cslot(gi + 1), w * step_delta<OP>(Gc.v, Gn.v, F.v));
+              if (w != T(0) && !(Gc.tn == t)) atomicAdd(&B.grad[2 * (coff + gi + 1)], w * step_delta<OP>(Gc.v, Gn.v, F.v));
               ++gi;
               Gc = Gn;
             }
             t = tn;
           }
           if (w != T(0)) atomicAdd(&sg[2 * fi + 1], w * accF);
-          if (w != T(0)) atomicAdd(cslot(gi) + 1, w * accG);
+          if (w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
           __syncwarp();
           for (uint32_t k = lane; k < rlen; k += 32)
           {
@@ -211,18 +196,6 @@ namespace sbg
         }
       }
       __syncthreads();
-      if (cshared)
-      {
-        // flush the item's column gradients (lane j owns column j's slots)
-        if (cvalid)
-          for (uint32_t k = warp; k < clen; k += blockDim.x >> 5)
-          {
-            const T gt = cgrad[((size_t)k * 32 + lane) * 2], gv = cgrad[((size_t)k * 32 + lane) * 2 + 1];
-            if (gt != T(0)) atomicAdd(&B.grad[2 * (coff + k)], gt);
-            if (gv != T(0)) atomicAdd(&B.grad[2 * (coff + k) + 1], gv);
-          }
-        __syncthreads();
-      }
     }
   }
 
@@ -288,13 +261,8 @@ namespace sbg
     B.queue = static_cast<unsigned long long*>(queue);
     B.row_cap = lmax;
     const int warps = 16;
-    const size_t row_bytes = (size_t)warps * lmax * 2 * sizeof(T);
-    if (row_bytes + 2048 > dev.smem_optin) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
-    // column-gradient block: as long as the rest of shared memory allows
-    const size_t spare = dev.smem_optin - 2048 - row_bytes;
-    B.col_cap = (uint32_t)std::min<size_t>(lmax, spare / (32 * 2 * sizeof(T)));
-    if (B.col_cap < 16) B.col_cap = 0;
-    const size_t smem = row_bytes + (size_t)B.col_cap * 32 * 2 * sizeof(T);
+    const size_t smem = (size_t)warps * lmax * 2 * sizeof(T);
+    if (smem + 2048 > dev.smem_optin) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
     uint32_t q = 1;
     for (uint32_t cand = 8; cand >= 1; cand /= 2)
       if (tri_item_count(0, n, cand, ceil_div_u64(n, 32)) >= (uint64_t)dev.sms * 6) { q = cand; break; }
