@@ -36,8 +36,8 @@ def test_factories_match_oracle(tmp_path):
         got.setdefault((tag, key), []).append(float(val))
     for tag, dt, tol in (("f32", np.float32, 1e-5), ("f64", np.float64, 1e-12)):
         pts, off = _five(dt)
-        cp, co = pts[6:], (off[2:] - off[2]).astype(np.uint64)
-        rp, ro = pts[:6], off[:3]
+        cp, co = pts[int(off[2]):], (off[2:] - off[2]).astype(np.uint64)
+        rp, ro = pts[:int(off[2])], off[:3]
         want = {
             "l1": orc.evaluate(pts, off),
             "l2": orc.evaluate(pts, off, op=orc.OP_LP, p=2.0),
