@@ -202,7 +202,7 @@ extern "C"
     return guarded([&] {
       if (warps < 0 || warps > 32) throw Error(ST_INVALID_ARGUMENT, "warps must be in [0, 32]");
       if (row_chunk < 0 || row_chunk > 1024) throw Error(ST_INVALID_ARGUMENT, "row_chunk must be in [0, 1024]");
-      if (variant < 0 || variant > 4) throw Error(ST_INVALID_ARGUMENT, "variant must be in [0, 4]");
+      if (variant < 0 || variant > 5) throw Error(ST_INVALID_ARGUMENT, "variant must be in [0, 5]");
       if (order < 0 || order > 2) throw Error(ST_INVALID_ARGUMENT, "order must be 0, 1 or 2");
       settings().warps.store(warps);
       settings().rowChunk.store(row_chunk);

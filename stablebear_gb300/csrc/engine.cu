@@ -174,7 +174,7 @@ namespace sbg
     const int want_w = settings().warps.load();
     // Shared-memory variants (rows and columns staged): the most warps that fit.
     int warps = 0;
-    if (variant == 0 || variant == 1 || variant == 3)
+    if (variant == 0 || variant == 1 || variant == 3 || variant == 5)
     {
       const int cands[] = {32, 24, 16, 12, 8, 4};
       for (int w : cands)
@@ -183,14 +183,14 @@ namespace sbg
         if (smem_for(w) <= usable) { warps = w; break; }
       }
     }
-    if ((variant == 1 || variant == 3) && warps == 0)
+    if ((variant == 1 || variant == 3 || variant == 5) && warps == 0)
       throw Error(ST_INVALID_ARGUMENT, "shared-memory variant requested but the PCFs do not fit in shared memory");
 
-    if ((variant == 0 && warps >= 16) || variant == 1 || variant == 3)
+    if ((variant == 0 && warps >= 16) || variant == 1 || variant == 3 || variant == 5)
     {
       pl.smem = true;
       pl.packed = false;
-      pl.kvar = variant == 3 ? 1 : 2;
+      pl.kvar = variant == 3 ? 1 : (variant == 5 ? 5 : 2);
       pl.warps = warps;
       pl.lmax_c = lmax_c;
       pl.row_cap = row_cap;

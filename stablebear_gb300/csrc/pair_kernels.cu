@@ -12,7 +12,10 @@ namespace sbg
   // FP64 adds cost more than a longer naive block loses (f64 sums of 16 terms
   // stay far below the 1e-12 target).
   template <typename T> struct Unroll;
-  template <> struct Unroll<float> { static constexpr int value = 8; };
+#ifndef SBG_F32_UNROLL
+#define SBG_F32_UNROLL 8
+#endif
+  template <> struct Unroll<float> { static constexpr int value = SBG_F32_UNROLL; };
   template <> struct Unroll<double> { static constexpr int value = 16; };
 
   namespace
@@ -132,6 +135,70 @@ namespace sbg
         "@p ld.shared.v2.f64 {%0, %1}, [%4];\n\t"
         "@!p ld.shared.v2.f64 {%2, %3}, [%5];\n\t}"
         : "+d"(fv), "+d"(ft), "+d"(gv), "+d"(gt), "+r"(af), "+r"(ag));
+  }
+
+  // One load per lane per step: every lane loads the element of the side it
+  // advances (address chosen by the comparison) in a single instruction with
+  // all 32 lanes active, and the loaded element is routed to that side.  Two
+  // half-populated predicated loads cost two partial wavefront sets each;
+  // one full load costs one set, at the price of the routing selects.
+  __device__ __forceinline__ void advance_shared_one(float& fv, float& ft, float& gv, float& gt, uint32_t& af,
+                                                     uint32_t& ag)
+  {
+    asm("{\n\t.reg .pred p;\n\t.reg .b32 a;\n\t.reg .f32 xv, xt;\n\t"
+        "setp.le.f32 p, %1, %3;\n\t"
+        "@p add.u32 %4, %4, 8;\n\t"
+        "@!p add.u32 %5, %5, 256;\n\t"
+        "selp.b32 a, %4, %5, p;\n\t"
+        "ld.shared.v2.f32 {xv, xt}, [a];\n\t"
+        "selp.f32 %0, xv, %0, p;\n\t"
+        "selp.f32 %1, xt, %1, p;\n\t"
+        "selp.f32 %2, %2, xv, p;\n\t"
+        "selp.f32 %3, %3, xt, p;\n\t}"
+        : "+f"(fv), "+f"(ft), "+f"(gv), "+f"(gt), "+r"(af), "+r"(ag));
+  }
+
+  __device__ __forceinline__ void advance_shared_one(double& fv, double& ft, double& gv, double& gt, uint32_t& af,
+                                                     uint32_t& ag)
+  {
+    asm("{\n\t.reg .pred p;\n\t.reg .b32 a;\n\t.reg .f64 xv, xt;\n\t.reg .s64 fa, ga;\n\t"
+        "mov.b64 fa, %1;\n\t"
+        "mov.b64 ga, %3;\n\t"
+        "setp.le.s64 p, fa, ga;\n\t"
+        "@p add.u32 %4, %4, 16;\n\t"
+        "@!p add.u32 %5, %5, 512;\n\t"
+        "selp.b32 a, %4, %5, p;\n\t"
+        "ld.shared.v2.f64 {xv, xt}, [a];\n\t"
+        "selp.f64 %0, xv, %0, p;\n\t"
+        "selp.f64 %1, xt, %1, p;\n\t"
+        "selp.f64 %2, %2, xv, p;\n\t"
+        "selp.f64 %3, %3, xt, p;\n\t}"
+        : "+d"(fv), "+d"(ft), "+d"(gv), "+d"(gt), "+r"(af), "+r"(ag));
+  }
+
+  template <typename T, int K, int U>
+  __device__ __forceinline__ T merge_smem_one(const Elem<T>* pf, const Elem<T>* pg, uint32_t steps, T p)
+  {
+    Elem<T> F = *pf;
+    Elem<T> G = *pg;
+    uint32_t af = (uint32_t)__cvta_generic_to_shared(pf);
+    uint32_t ag = (uint32_t)__cvta_generic_to_shared(pg);
+    T t = T(0), acc = T(0), comp = T(0);
+    const uint32_t nblk = (steps + U - 1) / U;
+    for (uint32_t b = 0; b < nblk; ++b)
+    {
+      T blk = T(0);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+      {
+        const T tn = earlier(F.tn, G.tn);
+        blk = PairOp<K>::acc(blk, tn - t, F.v, G.v, p);
+        t = tn;
+        advance_shared_one(F.v, F.tn, G.v, G.tn, af, ag);
+      }
+      kahan_add(acc, comp, blk);
+    }
+    return PairOp<K>::fin(acc - comp, p);
   }
 
   // Shared-memory merge with predicated loads.  pf: the warp's row buffer,
@@ -285,6 +352,7 @@ namespace sbg
             }
             __syncwarp();
             if (VAR == 1) res = merge_pair<T, K, U, 32, false>(rbuf, cols + lane, steps, rlen, p);
+            else if (VAR == 5) res = merge_smem_one<T, K, U>(rbuf, cols + lane, steps, p);
             else res = merge_smem_pred<T, K, U>(rbuf, cols + lane, steps, p);
             __syncwarp();
           }
@@ -546,6 +614,7 @@ namespace sbg
     dim3 g((unsigned)grid), b((unsigned)(warps * 32));
     if (variant == 1) return launch_op<T, 1>(opk, g, b, smem_bytes, s, L);
     if (variant == 2) return launch_op<T, 2>(opk, g, b, smem_bytes, s, L);
+    if (variant == 5) return launch_op<T, 5>(opk, g, b, smem_bytes, s, L);
     if (variant == 3) return launch_hybrid<T>(opk, g, b, smem_bytes, s, L);
     return launch_op<T, 0>(opk, g, b, 0, s, L);
   }

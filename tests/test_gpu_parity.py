@@ -196,10 +196,13 @@ def test_variants_orders_and_bands_agree():
         hyb = sb.pdist(X).data.copy()
         sb.set_tuning(variant=3, order=1)
         two = sb.pdist(X).data.copy()
+        sb.set_tuning(variant=5, order=1)
+        one = sb.pdist(X).data.copy()
     finally:
         sb.set_tuning()
     np.testing.assert_array_equal(hyb, base)
     np.testing.assert_array_equal(two, base)
+    np.testing.assert_array_equal(one, base)
     np.testing.assert_array_equal(gm, base)
     np.testing.assert_array_equal(banded, base)
     np.testing.assert_array_equal(small, base)
