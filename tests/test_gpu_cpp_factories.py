@@ -47,6 +47,9 @@ def test_factories_match_oracle(tmp_path):
         for key, w in want.items():
             g = np.array(got[(tag, key)])
             assert g.shape == w.shape
-            rel = np.abs(g - w) / np.maximum(np.abs(w), 1.0 if key == "k" else 1e-30)
+            fin = np.isfinite(w)
+            # PCF 3 never returns to zero: its distances are inf, as in the reference
+            np.testing.assert_array_equal(g[~fin], w[~fin])
+            rel = np.abs(g[fin] - w[fin]) / np.maximum(np.abs(w[fin]), 1.0 if key == "k" else 1e-30)
             assert rel.max() <= tol, (tag, key, g, w)
         assert got[(tag, "range_rejected")] == [1.0]
