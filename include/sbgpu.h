@@ -92,7 +92,7 @@ int sbg_get_device_verbose(void);
 /* Engine knobs (0 = automatic): warps per CTA, rows per work item / 32,
  * variant (1 shared-memory, 2 global-memory, 3 shared-memory with a two-load
  * walk, 4 hybrid: columns in shared memory, rows read through L1, 5
- * shared-memory with one unpredicated load per merge step), order
+ * shared-memory with the row as separate time and value arrays), order
  * (1 caller's, 2 sorted
  * by breakpoint count), output bytes per pipeline band. */
 int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes);

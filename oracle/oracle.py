@@ -90,6 +90,9 @@ def ref_lib():
             lib.sbref_schedule.restype = _U64
             lib.sbref_subdivide.argtypes = [_U64, _U64, _P, _U64]
             lib.sbref_subdivide.restype = _U64
+            for nm in ("sbref_matrix_body_f32", "sbref_matrix_body_f64"):
+                getattr(lib, nm).argtypes = [ctypes.c_int, _U64, _P, _P, _U64]
+                getattr(lib, nm).restype = _U64
             _ref = lib
     return _ref or None
 
@@ -264,3 +267,17 @@ def ref_subdivide(block, n_items):
     out = np.zeros(2 * cap, dtype=np.uint64)
     n = lib.sbref_subdivide(block, n_items, _ptr(out), cap)
     return out[: 2 * n].reshape(n, 2)
+
+
+def ref_matrix_body(kind, n, storage):
+    """Bytes the reference's ``write_element`` emits for a DistanceMatrix
+    (kind 1) or SymmetricMatrix (kind 2) holding ``storage``
+    (``include/sbear/io/compressed_matrix_io.hpp:10-20``)."""
+    lib = ref_lib()
+    storage = np.ascontiguousarray(storage)
+    fn = lib.sbref_matrix_body_f32 if storage.dtype == np.float32 else lib.sbref_matrix_body_f64
+    cap = 8 + storage.nbytes
+    out = np.zeros(cap, np.uint8)
+    nb = fn(kind, n, _ptr(storage), _ptr(out), cap)
+    assert nb == cap, (nb, cap)
+    return out.tobytes()

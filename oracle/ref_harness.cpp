@@ -8,6 +8,7 @@
 //   sbear/distance_matrix.hpp, sbear/symmetric_matrix.hpp (storage order)
 //   sbear/cuda/cuda_block_scheduler.hpp, sbear/algorithms/subdivide.hpp
 //   sbear/cuda/offset_data_manager.hpp
+//   sbear/io/compressed_matrix_io.hpp                   (matrix body on disk)
 // The 5-line integrate() body (matrix_integrate.hpp:18-29) and compute_row()
 // (matrix_integrate.hpp:80-90) are restated here, because matrix_integrate.hpp
 // itself pulls in taskflow, which the reference does not vendor.
@@ -24,8 +25,10 @@
 #include <sbear/cuda/cuda_block_scheduler.hpp>
 #include <sbear/algorithms/subdivide.hpp>
 #include <sbear/cuda/offset_data_manager.hpp>
+#include <sbear/io/compressed_matrix_io.hpp>
 
 #include <cstdint>
+#include <sstream>
 #include <cstring>
 #include <stdexcept>
 #include <limits>
@@ -108,6 +111,33 @@ namespace
         out[i * nc + j] = pair_value(rs[i], cs[j], op, p);
     return 0;
   }
+  // The body the reference writes for a DistanceMatrix (kind 1) or
+  // SymmetricMatrix (kind 2) (compressed_matrix_io.hpp:10-20), filled through
+  // the containers' public element access.
+  template <typename T>
+  uint64_t matrix_body(int kind, uint64_t n, const T* storage, unsigned char* out, uint64_t cap)
+  {
+    std::ostringstream os;
+    if (kind == 1)
+    {
+      sb::DistanceMatrix<T> m(n);
+      for (uint64_t i = 1; i < n; ++i)
+        for (uint64_t j = 0; j < i; ++j)
+          m(i, j) = storage[i * (i - 1) / 2 + j];
+      sb::io::detail::write_element(os, m);
+    }
+    else
+    {
+      sb::SymmetricMatrix<T> m(n);
+      for (uint64_t i = 0; i < n; ++i)
+        for (uint64_t j = 0; j <= i; ++j)
+          m(i, j) = storage[i * (i + 1) / 2 + j];
+      sb::io::detail::write_element(os, m);
+    }
+    const std::string b = os.str();
+    std::memcpy(out, b.data(), b.size() < cap ? b.size() : cap);
+    return b.size();
+  }
 }
 
 extern "C"
@@ -179,4 +209,11 @@ extern "C"
     for (size_t i = 0; i < v.size() && i < cap; ++i) { out[2 * i] = v[i].first; out[2 * i + 1] = v[i].second; }
     return v.size();
   }
+
+  // Returns the byte count of the body; copies at most cap bytes.
+  uint64_t sbref_matrix_body_f32(int kind, uint64_t n, const float* storage, unsigned char* out, uint64_t cap)
+  { return matrix_body(kind, n, storage, out, cap); }
+
+  uint64_t sbref_matrix_body_f64(int kind, uint64_t n, const double* storage, unsigned char* out, uint64_t cap)
+  { return matrix_body(kind, n, storage, out, cap); }
 }

@@ -18,6 +18,7 @@ from .system import (
     set_device_verbose, set_min_block_side, set_tuning, build_type, get_ngpus,
 )
 from .task import StoppableTask, EmptyTask
+from .io import save, load
 
 __all__ = [
     "Pcf", "PcfArray", "pcf32", "pcf64", "pcf32i", "pcf64i", "float32", "float64", "zeros",
@@ -26,7 +27,7 @@ __all__ = [
     "Distance_f32_f32", "Distance_f64_f64", "InnerProduct_f32_f32", "InnerProduct_f64_f64",
     "force_cpu", "set_block_size", "limit_cpus", "limit_gpus", "set_cuda_threshold", "get_cuda_threshold",
     "set_device_verbose", "set_min_block_side", "set_tuning", "build_type", "get_ngpus",
-    "StoppableTask", "EmptyTask",
+    "StoppableTask", "EmptyTask", "save", "load",
 ]
 
 __version__ = "0.1.0"

@@ -137,51 +137,53 @@ namespace sbg
         : "+d"(fv), "+d"(ft), "+d"(gv), "+d"(gt), "+r"(af), "+r"(ag));
   }
 
-  // One load per lane per step: every lane loads the element of the side it
-  // advances (address chosen by the comparison) in a single instruction with
-  // all 32 lanes active, and the loaded element is routed to that side.  Two
-  // half-populated predicated loads cost two partial wavefront sets each;
-  // one full load costs one set, at the price of the routing selects.
-  __device__ __forceinline__ void advance_shared_one(float& fv, float& ft, float& gv, float& gt, uint32_t& af,
-                                                     uint32_t& ag)
+  // Rows as two arrays (times, then values, `voff` bytes apart) instead of
+  // (v, tn) pairs.  All lanes of a warp read the same row at nearby
+  // positions; with 8-byte elements two lanes of a half-warp whose positions
+  // differ by a multiple of 16 hit the same bank pair, while with 4-byte
+  // words two positions collide only at a distance of 32 or more, so the two
+  // row loads are conflict-free in practice.  The column side keeps its
+  // 8-byte interleaved elements (lane j owns bank pair j mod 16).
+  __device__ __forceinline__ void advance_shared_soa(float& fv, float& ft, float& gv, float& gt, uint32_t& af,
+                                                     uint32_t voff, uint32_t& ag)
   {
-    asm("{\n\t.reg .pred p;\n\t.reg .b32 a;\n\t.reg .f32 xv, xt;\n\t"
+    asm("{\n\t.reg .pred p;\n\t.reg .b32 va;\n\t"
         "setp.le.f32 p, %1, %3;\n\t"
-        "@p add.u32 %4, %4, 8;\n\t"
+        "@p add.u32 %4, %4, 4;\n\t"
         "@!p add.u32 %5, %5, 256;\n\t"
-        "selp.b32 a, %4, %5, p;\n\t"
-        "ld.shared.v2.f32 {xv, xt}, [a];\n\t"
-        "selp.f32 %0, xv, %0, p;\n\t"
-        "selp.f32 %1, xt, %1, p;\n\t"
-        "selp.f32 %2, %2, xv, p;\n\t"
-        "selp.f32 %3, %3, xt, p;\n\t}"
-        : "+f"(fv), "+f"(ft), "+f"(gv), "+f"(gt), "+r"(af), "+r"(ag));
+        "add.u32 va, %4, %6;\n\t"
+        "@p ld.shared.f32 %1, [%4];\n\t"
+        "@p ld.shared.f32 %0, [va];\n\t"
+        "@!p ld.shared.v2.f32 {%2, %3}, [%5];\n\t}"
+        : "+f"(fv), "+f"(ft), "+f"(gv), "+f"(gt), "+r"(af), "+r"(ag)
+        : "r"(voff));
   }
 
-  __device__ __forceinline__ void advance_shared_one(double& fv, double& ft, double& gv, double& gt, uint32_t& af,
-                                                     uint32_t& ag)
+  __device__ __forceinline__ void advance_shared_soa(double& fv, double& ft, double& gv, double& gt, uint32_t& af,
+                                                     uint32_t voff, uint32_t& ag)
   {
-    asm("{\n\t.reg .pred p;\n\t.reg .b32 a;\n\t.reg .f64 xv, xt;\n\t.reg .s64 fa, ga;\n\t"
+    asm("{\n\t.reg .pred p;\n\t.reg .b32 va;\n\t.reg .s64 fa, ga;\n\t"
         "mov.b64 fa, %1;\n\t"
         "mov.b64 ga, %3;\n\t"
         "setp.le.s64 p, fa, ga;\n\t"
-        "@p add.u32 %4, %4, 16;\n\t"
+        "@p add.u32 %4, %4, 8;\n\t"
         "@!p add.u32 %5, %5, 512;\n\t"
-        "selp.b32 a, %4, %5, p;\n\t"
-        "ld.shared.v2.f64 {xv, xt}, [a];\n\t"
-        "selp.f64 %0, xv, %0, p;\n\t"
-        "selp.f64 %1, xt, %1, p;\n\t"
-        "selp.f64 %2, %2, xv, p;\n\t"
-        "selp.f64 %3, %3, xt, p;\n\t}"
-        : "+d"(fv), "+d"(ft), "+d"(gv), "+d"(gt), "+r"(af), "+r"(ag));
+        "add.u32 va, %4, %6;\n\t"
+        "@p ld.shared.f64 %1, [%4];\n\t"
+        "@p ld.shared.f64 %0, [va];\n\t"
+        "@!p ld.shared.v2.f64 {%2, %3}, [%5];\n\t}"
+        : "+d"(fv), "+d"(ft), "+d"(gv), "+d"(gt), "+r"(af), "+r"(ag)
+        : "r"(voff));
   }
 
+  // ft0: the warp's row times; the values follow `voff` bytes later.
   template <typename T, int K, int U>
-  __device__ __forceinline__ T merge_smem_one(const Elem<T>* pf, const Elem<T>* pg, uint32_t steps, T p)
+  __device__ __forceinline__ T merge_smem_soa(const T* ft0, uint32_t voff, const Elem<T>* pg, uint32_t steps, T p)
   {
-    Elem<T> F = *pf;
+    T fv = *reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(ft0) + voff);
+    T ft = *ft0;
     Elem<T> G = *pg;
-    uint32_t af = (uint32_t)__cvta_generic_to_shared(pf);
+    uint32_t af = (uint32_t)__cvta_generic_to_shared(ft0);
     uint32_t ag = (uint32_t)__cvta_generic_to_shared(pg);
     T t = T(0), acc = T(0), comp = T(0);
     const uint32_t nblk = (steps + U - 1) / U;
@@ -191,10 +193,10 @@ namespace sbg
 #pragma unroll
       for (int u = 0; u < U; ++u)
       {
-        const T tn = earlier(F.tn, G.tn);
-        blk = PairOp<K>::acc(blk, tn - t, F.v, G.v, p);
+        const T tn = earlier(ft, G.tn);
+        blk = PairOp<K>::acc(blk, tn - t, fv, G.v, p);
         t = tn;
-        advance_shared_one(F.v, F.tn, G.v, G.tn, af, ag);
+        advance_shared_soa(fv, ft, G.v, G.tn, af, voff, ag);
       }
       kahan_add(acc, comp, blk);
     }
@@ -232,7 +234,8 @@ namespace sbg
   // warp's row in shared memory; SMEM = false reads the packed segment layout
   // (pack_segments_kernel) from global memory through L1.
   // VAR: 0 global-memory variant, 1 shared memory with a two-load pointer
-  // walk, 2 shared memory with predicated one-side loads (the default).
+  // walk, 2 shared memory with predicated one-side loads (the default),
+  // 5 as 2 with the row held as separate time and value arrays.
   template <typename T, int K, int U, int VAR>
   __global__ void __launch_bounds__(1024, 1) pairs_kernel(const __grid_constant__ LaunchParams<T> L)
   {
@@ -338,21 +341,44 @@ namespace sbg
             const uint32_t pad_end = rlen + maxlc + U;
             if (pad_end > L.row_cap) continue;  // host sized row_cap; never expected
             const T* rp = Pp->rpts + 2 * roff;
-            for (uint32_t k = lane; k < rlen; k += 32)
-            {
-              const T tk = rp[2 * k], vk = rp[2 * k + 1];
-              rbuf[k].v = vk;
-              if (k > 0) rbuf[k - 1].tn = clamp_time(tk);
-            }
             const T vlast = rp[2 * (rlen - 1) + 1];
-            for (uint32_t k = rlen - 1 + lane; k < pad_end; k += 32)
+            if (VAR == 5)
             {
-              rbuf[k].v = vlast;
-              rbuf[k].tn = TM;
+              // times in [0, row_cap), values in [row_cap, 2 row_cap) of
+              // the warp's buffer (the same bytes as row_cap elements)
+              T* rt = reinterpret_cast<T*>(rbuf);
+              T* rv = rt + L.row_cap;
+              for (uint32_t k = lane; k < rlen; k += 32)
+              {
+                const T tk = rp[2 * k], vk = rp[2 * k + 1];
+                rv[k] = vk;
+                if (k > 0) rt[k - 1] = clamp_time(tk);
+              }
+              for (uint32_t k = rlen - 1 + lane; k < pad_end; k += 32)
+              {
+                rv[k] = vlast;
+                rt[k] = TM;
+              }
+            }
+            else
+            {
+              for (uint32_t k = lane; k < rlen; k += 32)
+              {
+                const T tk = rp[2 * k], vk = rp[2 * k + 1];
+                rbuf[k].v = vk;
+                if (k > 0) rbuf[k - 1].tn = clamp_time(tk);
+              }
+              for (uint32_t k = rlen - 1 + lane; k < pad_end; k += 32)
+              {
+                rbuf[k].v = vlast;
+                rbuf[k].tn = TM;
+              }
             }
             __syncwarp();
             if (VAR == 1) res = merge_pair<T, K, U, 32, false>(rbuf, cols + lane, steps, rlen, p);
-            else if (VAR == 5) res = merge_smem_one<T, K, U>(rbuf, cols + lane, steps, p);
+            else if (VAR == 5)
+              res = merge_smem_soa<T, K, U>(reinterpret_cast<const T*>(rbuf), L.row_cap * (uint32_t)sizeof(T),
+                                            cols + lane, steps, p);
             else res = merge_smem_pred<T, K, U>(rbuf, cols + lane, steps, p);
             __syncwarp();
           }

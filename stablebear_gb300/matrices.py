@@ -22,9 +22,6 @@ import numpy as np
 float32 = np.float32
 float64 = np.float64
 
-_FMT_MAGIC = b"SBGMAT1\0"
-
-
 def _check_dtype(dtype):
     dt = np.dtype(dtype if dtype is not None else np.float64)
     if dt not in (np.dtype(np.float32), np.dtype(np.float64)):
@@ -128,34 +125,31 @@ class _Condensed:
     def __repr__(self):
         return f"{type(self).__name__}(n={self._n}, dtype={self._data.dtype})"
 
-    # --- serialisation: u64 n then the storage (compressed_matrix_io.hpp:10-32) --
+    # --- serialisation: stablebear's binary format (see ``io.py``) ----------
 
     def to_bytes(self) -> bytes:
-        kind = b"D" if not self._diag else b"S"
-        code = b"f" if self._data.dtype == np.float32 else b"d"
-        head = _FMT_MAGIC + kind + code + np.uint64(self._n).tobytes()
-        return head + np.ascontiguousarray(self._data).tobytes()
+        from . import io as _sbio
+        return _sbio.to_bytes(self)
 
     @classmethod
     def from_bytes(cls, buf: bytes):
-        if buf[:8] != _FMT_MAGIC:
-            raise ValueError("not a serialised matrix")
-        kind, code = buf[8:9], buf[9:10]
-        if (kind == b"S") != cls._diag:
-            raise ValueError("serialised matrix has the other kind")
-        n = int(np.frombuffer(buf[10:18], dtype=np.uint64)[0])
-        dt = np.float32 if code == b"f" else np.float64
-        data = np.frombuffer(buf[18:], dtype=dt).copy()
-        return cls._wrap(n, data)
+        from . import io as _sbio
+        obj = _sbio.from_bytes(buf)
+        if type(obj) is not cls:
+            raise ValueError(f"serialised object is a {type(obj).__name__}, not a {cls.__name__}")
+        return obj
 
     def save(self, path):
-        with open(path, "wb") as fh:
-            fh.write(self.to_bytes())
+        from . import io as _sbio
+        _sbio.save(self, path)
 
     @classmethod
     def load(cls, path):
-        with open(path, "rb") as fh:
-            return cls.from_bytes(fh.read())
+        from . import io as _sbio
+        obj = _sbio.load(path)
+        if type(obj) is not cls:
+            raise ValueError(f"file holds a {type(obj).__name__}, not a {cls.__name__}")
+        return obj
 
     def __reduce__(self):
         return (type(self).from_bytes, (self.to_bytes(),))

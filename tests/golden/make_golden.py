@@ -113,6 +113,19 @@ def main():
         sched[f"blocks{k}"] = blocks
     np.savez(os.path.join(HERE, "reference_scheduler.npz"), **sched)
 
+    # The reference's on-disk body of small DistanceMatrix / SymmetricMatrix
+    # objects (u64 n, then the condensed storage).
+    rng = np.random.default_rng(5)
+    io_cases = {}
+    for dt, tag in ((np.float32, "f32"), (np.float64, "f64")):
+        for kind, n, name in ((1, 6, "dist"), (2, 5, "sym"), (1, 0, "dist_empty"), (2, 1, "sym_one")):
+            cnt = n * (n - 1) // 2 if kind == 1 else n * (n + 1) // 2
+            st = rng.uniform(0, 10, cnt).astype(dt)
+            io_cases[f"{name}_{tag}_storage"] = st
+            io_cases[f"{name}_{tag}_n"] = np.array([n], np.uint64)
+            io_cases[f"{name}_{tag}_body"] = np.frombuffer(orc.ref_matrix_body(kind, n, st), np.uint8)
+    np.savez(os.path.join(HERE, "reference_matrix_io.npz"), **io_cases)
+
 
 if __name__ == "__main__":
     main()
