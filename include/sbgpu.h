@@ -90,9 +90,10 @@ int sbg_limit_cpus(int n);
 int sbg_set_device_verbose(int on);
 int sbg_get_device_verbose(void);
 /* Engine knobs (0 = automatic): warps per CTA, rows per work item / 32,
- * variant (1 shared-memory, 2 global-memory, 3 shared-memory with a two-load
- * walk, 4 hybrid: columns in shared memory, rows read through L1, 5
- * shared-memory with the row as separate time and value arrays), order
+ * variant (1 shared-memory with 8-byte row elements, 2 global-memory, 3
+ * shared-memory with a two-load walk, 4 hybrid: columns in shared memory,
+ * rows read through L1, 5 shared-memory with the row as separate time and
+ * value arrays, the automatic choice when the PCFs fit), order
  * (1 caller's, 2 sorted
  * by breakpoint count), output bytes per pipeline band. */
 int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes);
@@ -268,6 +269,30 @@ int sbg_pairwise_device_noalloc(int dtype, int op, double p, int skip_mode,
 
 /* Number of output elements of a problem (n(n-1)/2, n(n+1)/2 or n_rows*n_cols). */
 uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols);
+
+/* ---- device-resident result containers ------------------------------------ */
+
+/* Dense rows [row_begin, row_end) of the n x n matrix held in condensed form
+ * on the device: skip_mode SBG_SKIP_LOWER_NODIAG for DistanceMatrix storage
+ * (zero diagonal), SBG_SKIP_LOWER for SymmetricMatrix storage.  Row i lands
+ * at dense + (i - row_begin) * ld (elements, ld >= n), on the caller's stream.
+ * Replaces DistanceMatrix / SymmetricMatrix `to_dense`
+ * (src/python/py_distance_matrix.hpp:37-49, py_symmetric_matrix.hpp), a
+ * serial host loop in the reference. */
+int sbg_condensed_to_dense_device(int dtype, int skip_mode, uint64_t n, const void* condensed, void* dense,
+                                  uint64_t ld, uint64_t row_begin, uint64_t row_end, void* stream);
+
+/* Condensed storage of a dense n x n device matrix (row stride ld), with the
+ * reference's `from_dense` checks (py_distance_matrix.hpp:50-73,
+ * py_symmetric_matrix.hpp:62-81) OR-ed into *flags (a device word the caller
+ * zeroes): SBG_FLAG_ASYMMETRIC, and for DistanceMatrix storage
+ * SBG_FLAG_DIAGONAL (a non-zero diagonal entry) and SBG_FLAG_NEGATIVE.  The
+ * storage is written whatever the flags say; the caller rejects it. */
+#define SBG_FLAG_ASYMMETRIC 1u
+#define SBG_FLAG_DIAGONAL 2u
+#define SBG_FLAG_NEGATIVE 4u
+int sbg_dense_to_condensed_device(int dtype, int skip_mode, uint64_t n, const void* dense, uint64_t ld,
+                                  void* condensed, unsigned int* flags, void* stream);
 
 #ifdef __cplusplus
 }

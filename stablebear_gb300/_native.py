@@ -29,6 +29,7 @@ STATUS_NAMES = {
 F32, F64 = 0, 1
 OP_L1, OP_LP, OP_L2_INNER = 0, 1, 2
 SKIP_NONE, SKIP_LOWER_NODIAG, SKIP_LOWER = 0, 1, 2
+FLAG_ASYMMETRIC, FLAG_DIAGONAL, FLAG_NEGATIVE = 1, 2, 4  # sbg_dense_to_condensed_device
 
 # Every symbol include/sbgpu.h declares, with (restype, argtypes).
 _P = ctypes.c_void_p
@@ -77,6 +78,8 @@ SIGNATURES = {
     "sbg_output_count": (_U64, [_I, _U64, _U64]),
     "sbg_measure_peak": (_I, [_I, ctypes.POINTER(_D)]),
     "sbg_enumerate_items": (_U64, [_I, _U64, _U64, _U64, _U64, ctypes.c_uint32, _P, _U64]),
+    "sbg_condensed_to_dense_device": (_I, [_I, _I, _U64, _P, _P, _U64, _U64, _U64, _P]),
+    "sbg_dense_to_condensed_device": (_I, [_I, _I, _U64, _P, _U64, _P, _P, _P]),
 }
 
 _lib = None

@@ -190,7 +190,7 @@ namespace sbg
     {
       pl.smem = true;
       pl.packed = false;
-      pl.kvar = variant == 3 ? 1 : (variant == 5 ? 5 : 2);
+      pl.kvar = variant == 3 ? 1 : (variant == 1 ? 2 : 5);  // auto: row times and values apart
       pl.warps = warps;
       pl.lmax_c = lmax_c;
       pl.row_cap = row_cap;

@@ -1,0 +1,262 @@
+// Device-resident consumers and producers of the condensed results.
+//
+// The reference turns a DistanceMatrix / SymmetricMatrix into a dense n x n
+// array with a serial host loop over all n^2 entries
+// (src/python/py_distance_matrix.hpp:37-49, py_symmetric_matrix.hpp), and
+// builds one from a dense array with another host loop that checks the
+// diagonal, sign and symmetry (py_distance_matrix.hpp:50-73).  Here both run
+// on the GPU over HBM-resident data:
+//
+//   condensed_to_dense: rows [row_begin, row_end) of the dense matrix;
+//   dense_to_condensed: the whole condensed storage, with the reference's
+//                       checks reported as flags.
+//
+// Both work on 32 x 32 tiles of the lower triangle.  A tile (a, b), a >= b,
+// is read once, coalesced along its columns, into shared memory and written
+// as the dense tile (a, b) and, transposed through shared memory, as the
+// dense tile (b, a): each condensed value is read once and both of its dense
+// copies are written once, which is the algorithmic traffic.  The kernels
+// are HBM-bound; CTAs loop over tiles (grid = a multiple of the SM count).
+#include "../../include/sbgpu.h"
+#include "sbg_internal.hpp"
+
+#include <cmath>
+
+namespace sbg
+{
+  namespace
+  {
+    constexpr int TILE = 32;
+    constexpr int ROWS = 8;  // thread rows per CTA: 32 x 8 threads, 4 rows each
+
+    __device__ __forceinline__ uint64_t cond_index(bool diag, uint64_t i, uint64_t j)
+    {
+      return diag ? i * (i + 1) / 2 + j : i * (i - 1) / 2 + j;  // i >= j (i > j without the diagonal)
+    }
+
+    // Tiles (a, b) with a >= b that touch the row band of block rows
+    // [Bb, Be): first every tile whose row block a lies in the band (b <= a),
+    // then every tile below the band whose column block b lies in it.
+    struct TileSet
+    {
+      uint64_t Bb, Be, nb;
+      uint64_t base;    // Bb (Bb + 1) / 2: tiles of the rows before the band
+      uint64_t count1;  // tiles with a in [Bb, Be)
+      uint64_t count;   // all tiles
+
+      __host__ __device__ void init(uint64_t Bb_, uint64_t Be_, uint64_t nb_)
+      {
+        Bb = Bb_; Be = Be_; nb = nb_;
+        base = Bb * (Bb + 1) / 2;
+        count1 = Be * (Be + 1) / 2 - base;
+        count = count1 + (Be - Bb) * (nb - Be);
+      }
+
+      __device__ void decode(uint64_t k, uint64_t* a, uint64_t* b) const
+      {
+        if (k < count1)
+        {
+          const uint64_t g = base + k;  // index in the full lower-triangle order
+          uint64_t r = (uint64_t)((sqrt(8.0 * (double)g + 1.0) - 1.0) * 0.5);
+          while (r * (r + 1) / 2 > g) --r;
+          while ((r + 1) * (r + 2) / 2 <= g) ++r;
+          *a = r;
+          *b = g - r * (r + 1) / 2;
+        }
+        else
+        {
+          const uint64_t k2 = k - count1, w = Be - Bb;
+          *a = Be + k2 / w;
+          *b = Bb + k2 % w;
+        }
+      }
+    };
+
+    template <typename T>
+    __global__ void __launch_bounds__(TILE * ROWS) condensed_to_dense_kernel(
+        const T* __restrict__ cond, uint64_t n, bool diag, T* __restrict__ dense, uint64_t ld,
+        uint64_t row_begin, uint64_t row_end, TileSet ts)
+    {
+      __shared__ T tile[TILE][TILE + 1];
+      const int tx = threadIdx.x, ty = threadIdx.y;
+      for (uint64_t k = blockIdx.x; k < ts.count; k += gridDim.x)
+      {
+        uint64_t a, b;
+        ts.decode(k, &a, &b);
+        const uint64_t i0 = a * TILE, j0 = b * TILE;
+        // Lower tile (a, b): row i = i0 + r, column j = j0 + tx.
+        for (int r = ty; r < TILE; r += ROWS)
+        {
+          const uint64_t i = i0 + r, j = j0 + tx;
+          T v = T(0);
+          if (i < n && j < n && (j < i || (diag && j == i))) v = cond[cond_index(diag, i, j)];
+          tile[r][tx] = v;
+        }
+        __syncthreads();
+        // Dense tile (a, b): rows of block a inside the band.
+        for (int r = ty; r < TILE; r += ROWS)
+        {
+          const uint64_t i = i0 + r, j = j0 + tx;
+          if (i >= row_begin && i < row_end && j < n)
+          {
+            // on the diagonal tile the upper half comes from the transposed lower half
+            const T v = (a != b || tx <= r) ? tile[r][tx] : tile[tx][r];
+            dense[(i - row_begin) * ld + j] = v;
+          }
+        }
+        // Dense tile (b, a), a > b: the transpose.
+        if (a != b)
+        {
+          for (int r = ty; r < TILE; r += ROWS)
+          {
+            const uint64_t i = j0 + r, j = i0 + tx;
+            if (i >= row_begin && i < row_end && j < n) dense[(i - row_begin) * ld + j] = tile[tx][r];
+          }
+        }
+        __syncthreads();
+      }
+    }
+
+    // Flags (bit set = violated somewhere): 1 not symmetric, 2 non-zero
+    // diagonal (distance matrices), 4 negative entry (distance matrices).
+    template <typename T>
+    __global__ void __launch_bounds__(TILE * ROWS) dense_to_condensed_kernel(
+        const T* __restrict__ dense, uint64_t n, uint64_t ld, bool diag, T* __restrict__ cond,
+        unsigned int* __restrict__ flags, TileSet ts)
+    {
+      __shared__ T upper[TILE][TILE + 1];
+      const int tx = threadIdx.x, ty = threadIdx.y;
+      unsigned int f = 0;
+      for (uint64_t k = blockIdx.x; k < ts.count; k += gridDim.x)
+      {
+        uint64_t a, b;
+        ts.decode(k, &a, &b);
+        const uint64_t i0 = a * TILE, j0 = b * TILE;
+        // The mirror tile (b, a), read coalesced and kept transposed.
+        for (int r = ty; r < TILE; r += ROWS)
+        {
+          const uint64_t i = j0 + r, j = i0 + tx;
+          upper[tx][r] = (i < n && j < n) ? dense[i * ld + j] : T(0);
+        }
+        __syncthreads();
+        for (int r = ty; r < TILE; r += ROWS)
+        {
+          const uint64_t i = i0 + r, j = j0 + tx;
+          if (i < n && j < n && j <= i)
+          {
+            const T v = dense[i * ld + j];
+            if (!(v == upper[r][tx])) f |= 1u;  // NaN counts as asymmetric, as != does in the reference
+            if (j == i)
+            {
+              if (diag) cond[cond_index(true, i, j)] = v;
+              else if (v != T(0)) f |= 2u;
+            }
+            else
+            {
+              if (!diag && v < T(0)) f |= 4u;
+              cond[cond_index(diag, i, j)] = v;
+            }
+          }
+        }
+        __syncthreads();
+      }
+      f = __reduce_or_sync(0xffffffffu, f);
+      if (f && (threadIdx.x & 31) == 0) atomicOr(flags, f);
+    }
+
+    int grid_for(uint64_t tiles)
+    {
+      const DeviceInfo d = device_info();
+      const uint64_t g = (uint64_t)d.sms * 8;  // 8 CTAs of 256 threads per SM
+      return (int)(tiles < g ? (tiles ? tiles : 1) : g);
+    }
+
+    template <typename F>
+    int abi_call(F&& f)
+    {
+      try
+      {
+        f();
+        set_last_error("");
+        return ST_OK;
+      }
+      catch (const Error& e)
+      {
+        set_last_error(e.what());
+        return e.status;
+      }
+      catch (const std::exception& e)
+      {
+        set_last_error(e.what());
+        return ST_INTERNAL;
+      }
+    }
+
+    void check_kind(int dtype, int skip)
+    {
+      if (dtype != SBG_F32 && dtype != SBG_F64) throw Error(ST_INVALID_ARGUMENT, "dtype must be SBG_F32 or SBG_F64");
+      if (skip != SBG_SKIP_LOWER_NODIAG && skip != SBG_SKIP_LOWER)
+        throw Error(ST_INVALID_ARGUMENT, "skip must be SBG_SKIP_LOWER_NODIAG (DistanceMatrix) or SBG_SKIP_LOWER "
+                                         "(SymmetricMatrix)");
+    }
+  }
+}
+
+using namespace sbg;
+
+extern "C"
+{
+  int sbg_condensed_to_dense_device(int dtype, int skip, uint64_t n, const void* condensed, void* dense, uint64_t ld,
+                                    uint64_t row_begin, uint64_t row_end, void* stream)
+  {
+    return abi_call([&] {
+      check_kind(dtype, skip);
+      if (row_end > n) row_end = n;
+      if (row_begin >= row_end) return;
+      if (ld < n) throw Error(ST_INVALID_ARGUMENT, "ld must be >= n");
+      if (!dense || (!condensed && output_count(skip, n, n) > 0))
+        throw Error(ST_INVALID_ARGUMENT, "null matrix pointer");
+      const uint64_t nb = ceil_div_u64(n, TILE);
+      TileSet ts;
+      ts.init(row_begin / TILE, ceil_div_u64(row_end, TILE), nb);
+      const bool diag = skip == SBG_SKIP_LOWER;
+      cudaStream_t st = (cudaStream_t)stream;
+      const dim3 block(TILE, ROWS);
+      const int grid = grid_for(ts.count);
+      if (dtype == SBG_F32)
+        condensed_to_dense_kernel<float><<<grid, block, 0, st>>>((const float*)condensed, n, diag, (float*)dense, ld,
+                                                                  row_begin, row_end, ts);
+      else
+        condensed_to_dense_kernel<double><<<grid, block, 0, st>>>((const double*)condensed, n, diag, (double*)dense,
+                                                                   ld, row_begin, row_end, ts);
+      SBG_CUDA(cudaGetLastError());
+    });
+  }
+
+  int sbg_dense_to_condensed_device(int dtype, int skip, uint64_t n, const void* dense, uint64_t ld, void* condensed,
+                                    unsigned int* flags, void* stream)
+  {
+    return abi_call([&] {
+      check_kind(dtype, skip);
+      if (!flags) throw Error(ST_INVALID_ARGUMENT, "flags must point to a device word");
+      if (n == 0) return;
+      if (ld < n) throw Error(ST_INVALID_ARGUMENT, "ld must be >= n");
+      if (!dense || (!condensed && output_count(skip, n, n) > 0))
+        throw Error(ST_INVALID_ARGUMENT, "null matrix pointer");
+      const uint64_t nb = ceil_div_u64(n, TILE);
+      TileSet ts;
+      ts.init(0, nb, nb);
+      cudaStream_t st = (cudaStream_t)stream;
+      const dim3 block(TILE, ROWS);
+      const int grid = grid_for(ts.count);
+      const bool diag = skip == SBG_SKIP_LOWER;
+      if (dtype == SBG_F32)
+        dense_to_condensed_kernel<float><<<grid, block, 0, st>>>((const float*)dense, n, ld, diag, (float*)condensed,
+                                                                  flags, ts);
+      else
+        dense_to_condensed_kernel<double><<<grid, block, 0, st>>>((const double*)dense, n, ld, diag,
+                                                                   (double*)condensed, flags, ts);
+      SBG_CUDA(cudaGetLastError());
+    });
+  }
+}

@@ -65,7 +65,7 @@ namespace sbg
     // Engine knobs (0 = automatic).
     std::atomic<int> warps{0};
     std::atomic<int> rowChunk{0};        // Q: rows per work item = 32 * Q
-    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory, 2 global-memory, 3 shared-memory pointer walk, 4 hybrid
+    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory (8-byte row elements), 2 global-memory, 3 shared-memory pointer walk, 4 hybrid, 5 shared-memory with row times and values apart
     std::atomic<int> order{0};           // 0 auto, 1 caller order, 2 length-sorted
     std::atomic<uint64_t> bandBytes{0};  // output bytes per pipeline band (0 = auto)
     std::atomic<int> outputMode{0};      // host results: 0 auto (staged), 1 staged copy, 2 direct stores (coherent hosts)

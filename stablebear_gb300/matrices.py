@@ -22,6 +22,17 @@ import numpy as np
 float32 = np.float32
 float64 = np.float64
 
+def _dense_input(array) -> np.ndarray:
+    a = np.asarray(array)
+    if a.dtype not in (np.float32, np.float64):
+        raise TypeError(f"Unsupported dtype {a.dtype}")
+    if a.ndim != 2:
+        raise ValueError("Expected a 2-D array")
+    if a.shape[0] != a.shape[1]:
+        raise ValueError("Expected a square array")
+    return a
+
+
 def _check_dtype(dtype):
     dt = np.dtype(dtype if dtype is not None else np.float64)
     if dt not in (np.dtype(np.float32), np.dtype(np.float64)):
@@ -178,18 +189,20 @@ class DistanceMatrix(_Condensed):
 
     @classmethod
     def from_dense(cls, array) -> "DistanceMatrix":
-        a = np.asarray(array)
-        if a.dtype not in (np.float32, np.float64):
-            raise TypeError(f"Unsupported dtype {a.dtype}")
-        if a.ndim != 2 or a.shape[0] != a.shape[1]:
-            raise ValueError("Input must be a square 2D array")
+        """Checks as the reference does (src/python/py_distance_matrix.hpp:50-73):
+        the diagonal first, then the strict upper triangle in row-major order,
+        where the first entry that is negative or differs from its mirror
+        decides the message."""
+        a = _dense_input(array)
         n = a.shape[0]
         if np.any(np.diag(a) != 0):
-            raise ValueError("Diagonal entries of a distance matrix must be zero")
-        if not np.array_equal(a, a.T):
-            raise ValueError("Input matrix must be symmetric")
-        if np.any(a < 0):
-            raise ValueError("Distance matrix entries must be nonnegative")
+            raise ValueError("Diagonal entries must be zero")
+        iu, ju = np.triu_indices(n, k=1)
+        up = a[iu, ju]
+        bad = (up < 0) | (up != a[ju, iu])
+        if bad.any():
+            k = int(np.argmax(bad))
+            raise ValueError("Entries must be nonnegative" if up[k] < 0 else "Matrix must be symmetric")
         rows, cols = np.tril_indices(n, k=-1)
         return cls._wrap(n, np.ascontiguousarray(a[rows, cols]))
 
@@ -209,13 +222,10 @@ class SymmetricMatrix(_Condensed):
 
     @classmethod
     def from_dense(cls, array) -> "SymmetricMatrix":
-        a = np.asarray(array)
-        if a.dtype not in (np.float32, np.float64):
-            raise TypeError(f"Unsupported dtype {a.dtype}")
-        if a.ndim != 2 or a.shape[0] != a.shape[1]:
-            raise ValueError("Input must be a square 2D array")
+        """As the reference (src/python/py_symmetric_matrix.hpp:62-81)."""
+        a = _dense_input(array)
         if not np.array_equal(a, a.T):
-            raise ValueError("Input matrix must be symmetric")
+            raise ValueError("Matrix must be symmetric")
         n = a.shape[0]
         rows, cols = np.tril_indices(n)
         return cls._wrap(n, np.ascontiguousarray(a[rows, cols]))
