@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--cpu-sample-rows", type=int, default=0, help="rows in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="large", choices=["large", "plain", "stable_rank", "batched", "fwdbwd"],
+    ap.add_argument("--config", default="large",
+                    choices=["large", "plain", "stable_rank", "batched", "fwdbwd", "dense"],
                     help="large: the headline workload; the others print their own report line")
     return ap.parse_args()
 
@@ -69,6 +70,17 @@ def _time_device(fn, steps, warmup):
 def _device_problem(pts, off):
     import torch
     return torch.from_numpy(pts).cuda(), torch.from_numpy(off.astype(np.int64)).cuda()
+
+
+def _hbm_peak():
+    """HBM copy bandwidth (GB/s) measured on the GB300s, else the
+    earlier single measurement."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback (6.8 TB/s, one earlier GB300 measurement)"
 
 
 def run_aux(args):
@@ -195,6 +207,36 @@ def run_aux(args):
                          "backward_over_forward": (ms_fb - ms_f) / ms_f}
         rep.update({"workload": "N=4096 f32, L~U{16..512}, upstream G symmetric N(0,1); grads w.r.t. values and times",
                     "segments_kernel": synthetic.segment_count(off, pts, 2)})
+    elif args.config == "dense":
+        from stablebear_gb300 import device as dev
+        n = args.n
+        cnt = n * (n - 1) // 2
+        g = torch.Generator("cuda").manual_seed(0)
+        cond = torch.rand(cnt, device="cuda", generator=g)
+        dense = torch.empty((n, n), device="cuda")
+        hbm, src = _hbm_peak()
+        to_dense = lambda: dev.condensed_to_dense(cond, n, "distance", out=dense)
+        ms_d = _time_device(to_dense, max(3, args.steps), max(3, args.warmup))
+        # spot check: rows against the condensed storage
+        rows = [0, 1, n // 2, n - 1]
+        errs = 0
+        for i in rows:
+            r = dense[i].cpu().numpy()
+            lo = cond[i * (i - 1) // 2: i * (i - 1) // 2 + i].cpu().numpy() if i else np.zeros(0, np.float32)
+            col = np.array([cond[j * (j - 1) // 2 + i].item() for j in range(i + 1, min(n, i + 65))], np.float32)
+            errs += int(not (np.array_equal(r[:i], lo) and r[i] == 0 and np.array_equal(r[i + 1:i + 1 + len(col)], col)))
+        ms_c = _time_device(lambda: dev.dense_to_condensed(dense, "distance", check=False), max(3, args.steps),
+                            max(3, args.warmup))
+        back_ok = bool(torch.equal(dev.dense_to_condensed(dense, "distance"), cond))
+        bytes_d = cnt * 4 + n * n * 4     # read each condensed value once, write both dense copies
+        bytes_c = n * n * 4 + cnt * 4     # read the dense matrix once, write the condensed storage
+        rep.update({"workload": f"DistanceMatrix N={n} f32 in HBM: condensed -> dense and back",
+                    "condensed_to_dense": {"ms": ms_d, "algorithmic_bytes": bytes_d, "gbs": bytes_d / ms_d / 1e6,
+                                           "frac_of_hbm_peak": bytes_d / ms_d / 1e6 / hbm, "rows_checked": len(rows),
+                                           "row_mismatches": errs},
+                    "dense_to_condensed": {"ms": ms_c, "algorithmic_bytes": bytes_c, "gbs": bytes_c / ms_c / 1e6,
+                                           "frac_of_hbm_peak": bytes_c / ms_c / 1e6 / hbm, "round_trip_equal": back_ok},
+                    "hbm_peak_gbs": hbm, "hbm_peak_source": src})
     print(json.dumps(rep), flush=True)
 
 

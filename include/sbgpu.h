@@ -294,6 +294,20 @@ int sbg_condensed_to_dense_device(int dtype, int skip_mode, uint64_t n, const vo
 int sbg_dense_to_condensed_device(int dtype, int skip_mode, uint64_t n, const void* dense, uint64_t ld,
                                   void* condensed, unsigned int* flags, void* stream);
 
+/* ---- single-PCF integrals --------------------------------------------------- */
+
+/* out[i] = ||f_i||_p over [0, inf) for the n PCFs of the CSR (p >= 1): the
+ * reference's l1_norm (p == 1) and lp_norm (any other p, through pow)
+ * (include/sbear/algorithms/functional/apply_functional.hpp:63-100, bound as
+ * Norms_f32_f32 / Norms_f64_f64 .lpnorm_l1 / .lpnorm_lp in
+ * src/python/functional/py_norms.cpp:24-56).  Device pointers, caller's
+ * stream; the CSR is not validated. */
+int sbg_lp_norm_device(int dtype, double p, const void* points, const uint64_t* offsets, uint64_t n, void* out,
+                       void* stream);
+/* The same from host memory, blocking, with the input checks of the
+ * pairwise entries. */
+int sbg_lp_norm_host(int dtype, double p, const void* points, const uint64_t* offsets, uint64_t n, void* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,8 @@ def _load():
         lib.sbo_integrate_dd_f64.restype = ctypes.c_double
         lib.sbo_count_total_segments.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, _U64, _P, _P, _U64]
         lib.sbo_count_total_segments.restype = _U64
+        lib.sbo_lp_norm.argtypes = [ctypes.c_int, ctypes.c_double, _P, _P, _U64, _P]
+        lib.sbo_lp_norm.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -90,6 +92,10 @@ def ref_lib():
             lib.sbref_schedule.restype = _U64
             lib.sbref_subdivide.argtypes = [_U64, _U64, _P, _U64]
             lib.sbref_subdivide.restype = _U64
+            lib.sbref_lp_norm_f32.argtypes = [_P, _U64, ctypes.c_float]
+            lib.sbref_lp_norm_f32.restype = ctypes.c_float
+            lib.sbref_lp_norm_f64.argtypes = [_P, _U64, ctypes.c_double]
+            lib.sbref_lp_norm_f64.restype = ctypes.c_double
             for nm in ("sbref_matrix_body_f32", "sbref_matrix_body_f64"):
                 getattr(lib, nm).argtypes = [ctypes.c_int, _U64, _P, _P, _U64]
                 getattr(lib, nm).restype = _U64
@@ -281,3 +287,25 @@ def ref_matrix_body(kind, n, storage):
     nb = fn(kind, n, _ptr(storage), _ptr(out), cap)
     assert nb == cap, (nb, cap)
     return out.tobytes()
+
+
+def lp_norm(points, offsets, p=1.0):
+    """Lp norm of every PCF (the restatement of l1_norm / lp_norm)."""
+    lib = _load()
+    pts, off = _csr(points, offsets)
+    n = len(off) - 1
+    out = np.zeros(n, dtype=pts.dtype)
+    lib.sbo_lp_norm(_dtype_code(pts), float(p), _ptr(pts), _ptr(off), n, _ptr(out))
+    return out
+
+
+def ref_lp_norm(points, offsets, p=1.0):
+    """Lp norm of every PCF through the reference's own iterate_segments."""
+    lib = ref_lib()
+    pts, off = _csr(points, offsets)
+    fn = lib.sbref_lp_norm_f32 if pts.dtype == np.float32 else lib.sbref_lp_norm_f64
+    out = np.zeros(len(off) - 1, dtype=pts.dtype)
+    for i in range(len(off) - 1):
+        a, b = int(off[i]), int(off[i + 1])
+        out[i] = fn(_ptr(pts[a:b]), b - a, p)
+    return out

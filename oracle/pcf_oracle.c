@@ -496,3 +496,47 @@ int sbo_gradient_f64(const double* pts, const uint64_t* off, uint64_t n, int op,
   }
   return 0;
 }
+
+/* ---------------------------------------------------------------------- */
+/* Single-PCF Lp norms: l1_norm / lp_norm                                   */
+/* (include/sbear/algorithms/functional/apply_functional.hpp:63-100) over   */
+/* iterate_segments with a = 0, b = max (iterate_rectangles.hpp:106-155):   */
+/* start at the last breakpoint with t <= a; segment [t_prev, min(t, b))    */
+/* with the previous value; stop after a segment that reaches b; otherwise  */
+/* a last segment [t_last, b).  Naive in-order sum; p == 1 uses |v|, any    */
+/* other p pow(|v|, p) and a final pow(sum, 1/p).                           */
+/* ---------------------------------------------------------------------- */
+
+#define SBO_DEFINE_NORM(T, SUF, ABS, POW, TMAX)                                             \
+  static T sbo_norm_one_##SUF(const T* f, uint64_t lf, T p)                                 \
+  {                                                                                         \
+    const T b = TMAX;                                                                       \
+    uint64_t prev = 0;                                                                      \
+    T out = (T)0;                                                                           \
+    if (lf == 0) return (T)0;                                                               \
+    while (prev + 1 < lf && f[2 * (prev + 1)] <= (T)0) ++prev;                              \
+    T tprev = (T)0, vprev = f[2 * prev + 1];                                                \
+    for (uint64_t k = prev + 1; k < lf; ++k) {                                              \
+      T tnext = f[2 * k] < b ? f[2 * k] : b;                                                \
+      out += (tnext - tprev) * (p == (T)1 ? ABS(vprev) : POW(ABS(vprev), p));               \
+      if (tnext >= b) return p == (T)1 ? out : POW(out, (T)1 / p);                          \
+      tprev = f[2 * k];                                                                     \
+      vprev = f[2 * k + 1];                                                                 \
+    }                                                                                       \
+    out += (b - tprev) * (p == (T)1 ? ABS(vprev) : POW(ABS(vprev), p));                     \
+    return p == (T)1 ? out : POW(out, (T)1 / p);                                            \
+  }
+
+SBO_DEFINE_NORM(float, f32, fabsf, powf, FLT_MAX)
+SBO_DEFINE_NORM(double, f64, fabs, pow, DBL_MAX)
+
+int sbo_lp_norm(int dtype, double p, const void* pts, const uint64_t* off, uint64_t n, void* out)
+{
+  for (uint64_t i = 0; i < n; ++i) {
+    if (dtype == 0)
+      ((float*)out)[i] = sbo_norm_one_f32((const float*)pts + 2 * off[i], off[i + 1] - off[i], (float)p);
+    else
+      ((double*)out)[i] = sbo_norm_one_f64((const double*)pts + 2 * off[i], off[i + 1] - off[i], p);
+  }
+  return 0;
+}

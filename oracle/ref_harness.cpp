@@ -27,6 +27,7 @@
 #include <sbear/cuda/offset_data_manager.hpp>
 #include <sbear/io/compressed_matrix_io.hpp>
 
+#include <cmath>
 #include <cstdint>
 #include <sstream>
 #include <cstring>
@@ -208,6 +209,32 @@ extern "C"
     auto v = sb::subdivide(blockSize, nItems);
     for (size_t i = 0; i < v.size() && i < cap; ++i) { out[2 * i] = v[i].first; out[2 * i + 1] = v[i].second; }
     return v.size();
+  }
+
+  // l1_norm / lp_norm (apply_functional.hpp:63-100, restated: that header
+  // pulls in taskflow) over the reference's own iterate_segments.
+  double sbref_lp_norm_f64(const double* f, uint64_t lf, double p)
+  {
+    auto pts = to_points(f, lf);
+    double out = 0.0;
+    sb::iterate_segments(pts.cbegin(), pts.cend(), 0.0, std::numeric_limits<double>::max(),
+                         [&out, p](const auto& seg) {
+                           const double a = std::abs(seg.value);
+                           out += (seg.right - seg.left) * (p == 1.0 ? a : std::pow(a, p));
+                         });
+    return p == 1.0 ? out : std::pow(out, 1.0 / p);
+  }
+
+  float sbref_lp_norm_f32(const float* f, uint64_t lf, float p)
+  {
+    auto pts = to_points(f, lf);
+    float out = 0.0f;
+    sb::iterate_segments(pts.cbegin(), pts.cend(), 0.0f, std::numeric_limits<float>::max(),
+                         [&out, p](const auto& seg) {
+                           const float a = std::abs(seg.value);
+                           out += (seg.right - seg.left) * (p == 1.0f ? a : std::pow(a, p));
+                         });
+    return p == 1.0f ? out : std::pow(out, 1.0f / p);
   }
 
   // Returns the byte count of the body; copies at most cap bytes.

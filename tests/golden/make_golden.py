@@ -126,6 +126,23 @@ def main():
             io_cases[f"{name}_{tag}_body"] = np.frombuffer(orc.ref_matrix_body(kind, n, st), np.uint8)
     np.savez(os.path.join(HERE, "reference_matrix_io.npz"), **io_cases)
 
+    # Lp norms through the reference's own iterate_segments: ragged PCFs with
+    # tails, repeated t = 0 breakpoints and ties, p in {1, 1.5, 2, 3}.
+    norms = {}
+    for dt, tag in ((np.float32, "f32"), (np.float64, "f64")):
+        pts, off = _ragged(60, 1, 40, dt, 21)
+        pts = _with_tails(pts, off, 22)
+        pts = _with_ties(pts, off, 23, dt) if tag == "f64" else pts
+        # a PCF whose first two breakpoints sit at t = 0
+        a = int(off[3])
+        if int(off[4]) - a >= 3:
+            pts[a + 1, 0] = 0
+        norms[f"{tag}_points"] = pts
+        norms[f"{tag}_offsets"] = off
+        for p in (1.0, 1.5, 2.0, 3.0):
+            norms[f"{tag}_p{p}"] = orc.ref_lp_norm(pts, off, p)
+    np.savez(os.path.join(HERE, "reference_norms.npz"), **norms)
+
 
 if __name__ == "__main__":
     main()

@@ -1,9 +1,12 @@
 """The oracle pinned against the reference: its own tests' known answers and
 the golden fixtures produced by the reference's code (CPU only)."""
+import os
+
 import numpy as np
 import pytest
 
 from oracle import oracle as orc
+from tests.conftest import GOLDEN
 
 F32 = np.float32
 F64 = np.float64
@@ -199,3 +202,31 @@ def test_oracle_gradient_matches_central_differences(op, mode, p):
             assert abs(fd - g[k, c]) <= 1e-6 * max(1.0, abs(fd)), (k, c, fd, g[k, c])
             checked += 1
     assert checked > 40
+
+
+# ---- single-PCF Lp norms ------------------------------------------------------
+
+@pytest.mark.parametrize("tag", ["f32", "f64"])
+@pytest.mark.parametrize("p", [1.0, 1.5, 2.0, 3.0])
+def test_norm_oracle_matches_reference_bitwise(tag, p):
+    d = np.load(os.path.join(GOLDEN, "reference_norms.npz"))
+    got = orc.lp_norm(d[f"{tag}_points"], d[f"{tag}_offsets"], p)
+    np.testing.assert_array_equal(got, d[f"{tag}_p{p}"])
+
+
+def test_norm_known_answers():
+    """The reference's norm test cases (test/python/test_norms.py,
+    test_norms_extended.py), restated."""
+    pcfs = [[[0, 10], [2, 5], [4, 0]], [[0, 5], [3, 6], [5, 5], [8, 0]], [[0, 12], [3, 0]],
+            [[0, 50], [0.5, 0]], [[0, 0]], [[0, 2], [3, 0]]]
+    pts = np.concatenate([np.array(x, np.float64) for x in pcfs])
+    off = np.zeros(len(pcfs) + 1, np.uint64)
+    np.cumsum([len(x) for x in pcfs], out=off[1:])
+    np.testing.assert_allclose(orc.lp_norm(pts, off, 1.0), [30, 42, 36, 25, 0, 6], rtol=1e-12)
+    one = lambda x, p: orc.lp_norm(np.array(x, np.float64), np.array([0, len(x)], np.uint64), p)[0]
+    assert one([[0, 3], [4, 0]], 2.0) == pytest.approx(6.0)
+    assert one([[0, 1], [1, 2], [2, 0]], 2.0) == pytest.approx(np.sqrt(5.0))
+    assert one([[0, -2], [1, 0]], 3.0) == pytest.approx(2.0)
+    assert one([[0, 0]], 2.0) == 0.0
+    # repeated t = 0: the walk starts at the last breakpoint with t <= 0
+    assert one([[0, 7], [0, 1], [2, 0]], 1.0) == 2.0
