@@ -258,25 +258,6 @@ namespace sbg
     return s;
   }
 
-  // Merge steps a warp spends on one row against each 32-column group,
-  // summed over groups, in the given column order (the warp-uniform step
-  // count is L_row + max over the group - 1).
-  static double group_cost(const uint64_t* off, uint64_t n, const uint32_t* order)
-  {
-    double cost = 0.0;
-    for (uint64_t g0 = 0; g0 < n; g0 += 32)
-    {
-      uint64_t mx = 0;
-      for (uint64_t j = g0; j < std::min<uint64_t>(n, g0 + 32); ++j)
-      {
-        uint64_t c = order ? order[j] : j;
-        mx = std::max<uint64_t>(mx, off[c + 1] - off[c]);
-      }
-      cost += 32.0 * (double)mx;
-    }
-    return cost;
-  }
-
   static std::vector<uint32_t> length_order(const uint64_t* off, uint64_t n)
   {
     std::vector<uint32_t> perm(n);
@@ -391,6 +372,31 @@ namespace sbg
     const Plan pl = make_plan<T>(mode, rows.n, cs.n, ls, ls, dev);
     if (row_begin % (32ull * pl.q) != 0)
       throw Error(ST_INVALID_ARGUMENT, "row_begin must be a multiple of the row chunk (32*q)");
+
+    // Processing order: by breakpoint count, computed on the stream, when
+    // the call covers the whole matrix (a band in caller order owns one
+    // contiguous output range; in another order it would not) and neither
+    // the caller nor the order setting fixed one.  The permutation is the
+    // one the host entry uses, so both give the same bits.
+    std::unique_ptr<AsyncBuf<T>> order_buf;
+    const bool whole = row_begin == 0 && row_end == rows.n && out_base == 0;
+    if (!rperm && !cperm && whole && settings().order.load() != 1 && rows.n <= 0xffffffffull &&
+        cs.n <= 0xffffffffull)
+    {
+      const uint64_t nr = rows.n, nc = (mode == MODE_CROSS) ? cs.n : 0;
+      const size_t perm_bytes = ((nr + nc) * sizeof(uint32_t) + 255) / 256 * 256;
+      const size_t key_bytes = std::max(length_order_scratch_bytes(nr), length_order_scratch_bytes(nc));
+      order_buf.reset(new AsyncBuf<T>(perm_bytes + key_bytes, st));
+      uint32_t* rp = static_cast<uint32_t*>(order_buf->p);
+      void* keys = static_cast<char*>(order_buf->p) + perm_bytes;
+      length_order_device(rows.off, nr, rp, keys, st);
+      rperm = rp;
+      if (mode == MODE_CROSS)
+      {
+        length_order_device(cs.off, nc, rp + nr, keys, st);
+        cperm = rp + nr;
+      }
+    }
 
     ProblemDesc<T> d{};
     d.rpts = rows.pts; d.roff = rows.off; d.rperm = rperm; d.nr = rows.n;
@@ -579,8 +585,9 @@ namespace sbg
     drows.upload(rows, compute.s);
     if (mode == MODE_CROSS) dcols.upload(cs, compute.s);
 
-    // Processing order: length-sorted when grouping by length saves work and
-    // the whole output stays in one device buffer.
+    // Processing order: length-sorted (unless the order setting asks for the
+    // caller's) when the whole output stays in one device buffer.  The
+    // permutation is the one the device entry computes on the GPU.
     size_t freeb = 0, totalb = 0;
     SBG_CUDA(cudaMemGetInfo(&freeb, &totalb));
     const size_t out_bytes = (size_t)total * sizeof(T);
@@ -590,14 +597,9 @@ namespace sbg
     bool sorted = false;
     if (order != 1 && out_bytes <= budget && rows.n <= 0xffffffffull && cs.n <= 0xffffffffull)
     {
-      std::vector<uint32_t> co = length_order(cs.off, cs.n);
-      const double nat = group_cost(cs.off, cs.n, nullptr), srt = group_cost(cs.off, cs.n, co.data());
-      if (order == 2 || nat > 1.08 * srt)
-      {
-        sorted = true;
-        cperm = std::move(co);
-        rperm = (mode == MODE_CROSS) ? length_order(rows.off, rows.n) : cperm;
-      }
+      sorted = true;
+      cperm = length_order(cs.off, cs.n);
+      rperm = (mode == MODE_CROSS) ? length_order(rows.off, rows.n) : cperm;
     }
     DeviceBuffer drperm, dcperm;
     if (sorted)

@@ -57,7 +57,8 @@ namespace sbg
         if (k < count1)
         {
           const uint64_t g = base + k;  // index in the full lower-triangle order
-          uint64_t r = (uint64_t)((sqrt(8.0 * (double)g + 1.0) - 1.0) * 0.5);
+          // FP32 estimate (FP64 is a slow pipe here), then exact correction
+          uint64_t r = (uint64_t)((sqrtf(8.0f * (float)g + 1.0f) - 1.0f) * 0.5f);
           while (r * (r + 1) / 2 > g) --r;
           while ((r + 1) * (r + 2) / 2 <= g) ++r;
           *a = r;
@@ -85,9 +86,11 @@ namespace sbg
         ts.decode(k, &a, &b);
         const uint64_t i0 = a * TILE, j0 = b * TILE;
         // Lower tile (a, b): row i = i0 + r, column j = j0 + tx.
+        const uint64_t j = j0 + tx;
+#pragma unroll
         for (int r = ty; r < TILE; r += ROWS)
         {
-          const uint64_t i = i0 + r, j = j0 + tx;
+          const uint64_t i = i0 + r;
           T v = T(0);
           if (i < n && j < n && (j < i || (diag && j == i))) v = cond[cond_index(diag, i, j)];
           tile[r][tx] = v;

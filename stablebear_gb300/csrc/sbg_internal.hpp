@@ -196,4 +196,12 @@ namespace sbg
 
   uint64_t output_count(int mode, uint64_t n_rows, uint64_t n_cols);
   uint64_t row_output_start(int mode, uint64_t row, uint64_t n_cols);
+
+  // Device-side length order (sort.cu): perm[i] = index of the PCF with the
+  // i-th smallest breakpoint count, ties by index.  `scratch` holds
+  // length_order_scratch_bytes(n) bytes.
+  uint64_t length_order_scratch_bytes(uint64_t n);
+  void length_order_device(const uint64_t* off, uint64_t n, uint32_t* perm, void* scratch, cudaStream_t st);
+  // Ascending bitonic sort of npad (a power of two) 64-bit keys in place.
+  void sort_keys_u64(uint64_t* keys, uint64_t npad, cudaStream_t st);
 }

@@ -1,0 +1,142 @@
+// Length order of a PCF set on the device: the permutation that visits PCFs
+// by increasing breakpoint count, ties by index (the same permutation as a
+// stable host sort by length).  Grouping columns of similar length keeps the
+// warp-uniform step count of the pair kernels close to the work each lane
+// does; the order is computed on the stream, with no host round trip.
+//
+// Keys (length << 32 | index) are unique, so a bitonic network (not stable
+// by itself) gives the one deterministic order.  The key array is padded to
+// a power of two with all-ones keys, which sort last.  Sorting network:
+// tiles of 2048 keys are sorted in shared memory; stages whose partner
+// distance is a tile or more run as one global compare-exchange pass each,
+// and the rest of every stage finishes inside the tiles again.
+#include "sbg_internal.hpp"
+
+#include <algorithm>
+
+namespace sbg
+{
+  namespace
+  {
+    constexpr int SORT_THREADS = 1024;
+    constexpr uint64_t SORT_TILE = 2 * SORT_THREADS;
+
+    __device__ __forceinline__ void cmp_swap(uint64_t& a, uint64_t& b, bool ascending)
+    {
+      if ((a > b) == ascending)
+      {
+        const uint64_t t = a;
+        a = b;
+        b = t;
+      }
+    }
+
+    // Stages k = k_first .. k_last (powers of two) with partner distances
+    // j = min(k / 2, j_first) .. 1, on one tile in shared memory.  The
+    // direction of a comparison comes from the global index.
+    __global__ void __launch_bounds__(SORT_THREADS) tile_stages_kernel(uint64_t* keys, uint64_t n, uint64_t tile,
+                                                                       uint64_t k_first, uint64_t k_last,
+                                                                       uint64_t j_first)
+    {
+      __shared__ uint64_t s[SORT_TILE];
+      const uint64_t base = (uint64_t)blockIdx.x * tile;
+      for (uint64_t i = threadIdx.x; i < tile; i += blockDim.x) s[i] = keys[base + i];
+      __syncthreads();
+      for (uint64_t k = k_first; k <= k_last; k <<= 1)
+      {
+        for (uint64_t j = (k / 2 < j_first ? k / 2 : j_first); j > 0; j >>= 1)
+        {
+          for (uint64_t t = threadIdx.x; t < tile / 2; t += blockDim.x)
+          {
+            const uint64_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));  // j is a power of two
+            const uint64_t g = base + i;
+            cmp_swap(s[i], s[i + j], (g & k) == 0);
+          }
+          __syncthreads();
+        }
+      }
+      for (uint64_t i = threadIdx.x; i < tile; i += blockDim.x) keys[base + i] = s[i];
+      (void)n;
+    }
+
+    // One compare-exchange pass of stage k at partner distance j over the
+    // whole array (n / 2 pairs).
+    __global__ void global_step_kernel(uint64_t* keys, uint64_t n, uint64_t j, uint64_t k)
+    {
+      const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+      if (t >= n / 2) return;
+      const uint64_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));  // j is a power of two
+      uint64_t a = keys[i], b = keys[i + j];
+      if ((a > b) == ((i & k) == 0))
+      {
+        keys[i] = b;
+        keys[i + j] = a;
+      }
+    }
+
+    __global__ void make_keys_kernel(const uint64_t* __restrict__ off, uint64_t n, uint64_t npad,
+                                     uint64_t* __restrict__ keys)
+    {
+      for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += (uint64_t)gridDim.x * blockDim.x)
+      {
+        if (i < n)
+        {
+          uint64_t len = off[i + 1] - off[i];
+          if (len > 0xffffffffull) len = 0xffffffffull;
+          keys[i] = (len << 32) | i;
+        }
+        else keys[i] = ~0ull;
+      }
+    }
+
+    __global__ void keys_to_perm_kernel(const uint64_t* __restrict__ keys, uint64_t n, uint32_t* __restrict__ perm)
+    {
+      for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        perm[i] = (uint32_t)(keys[i] & 0xffffffffull);
+    }
+  }
+
+  void sort_keys_u64(uint64_t* keys, uint64_t npad, cudaStream_t st)
+  {
+    if (npad < 2) return;
+    if ((npad & (npad - 1)) != 0) throw Error(ST_INTERNAL, "sort_keys_u64: length must be a power of two");
+    const uint64_t tile = npad < SORT_TILE ? npad : SORT_TILE;
+    const unsigned tiles = (unsigned)(npad / tile);
+    // every stage that fits in a tile
+    tile_stages_kernel<<<tiles, SORT_THREADS, 0, st>>>(keys, npad, tile, 2, tile, tile / 2);
+    SBG_CUDA(cudaGetLastError());
+    for (uint64_t k = 2 * tile; k <= npad; k <<= 1)
+    {
+      for (uint64_t j = k / 2; j >= tile; j >>= 1)
+      {
+        const uint64_t pairs = npad / 2;
+        global_step_kernel<<<(unsigned)((pairs + 255) / 256), 256, 0, st>>>(keys, npad, j, k);
+        SBG_CUDA(cudaGetLastError());
+      }
+      tile_stages_kernel<<<tiles, SORT_THREADS, 0, st>>>(keys, npad, tile, k, k, tile / 2);
+      SBG_CUDA(cudaGetLastError());
+    }
+  }
+
+  uint64_t length_order_scratch_bytes(uint64_t n)
+  {
+    uint64_t npad = 1;
+    while (npad < n) npad <<= 1;
+    return npad * sizeof(uint64_t);
+  }
+
+  void length_order_device(const uint64_t* off, uint64_t n, uint32_t* perm, void* scratch, cudaStream_t st)
+  {
+    if (n == 0) return;
+    if (n > 0xffffffffull) throw Error(ST_INVALID_ARGUMENT, "too many PCFs for a 32-bit processing order");
+    uint64_t npad = 1;
+    while (npad < n) npad <<= 1;
+    uint64_t* keys = static_cast<uint64_t*>(scratch);
+    const unsigned blocks = (unsigned)std::min<uint64_t>((npad + 255) / 256, 4096);
+    make_keys_kernel<<<blocks, 256, 0, st>>>(off, n, npad, keys);
+    SBG_CUDA(cudaGetLastError());
+    sort_keys_u64(keys, npad, st);
+    keys_to_perm_kernel<<<blocks, 256, 0, st>>>(keys, n, perm);
+    SBG_CUDA(cudaGetLastError());
+  }
+}

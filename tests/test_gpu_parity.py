@@ -240,8 +240,10 @@ def test_cdist_self_equals_pdist():
 
 
 def test_device_entry_matches_host_entry():
-    """sbg_pairwise_device on torch-owned device buffers, whole output and as
-    two row bands, equals the host pipeline bit for bit."""
+    """sbg_pairwise_device on torch-owned device buffers equals the host
+    pipeline bit for bit: the whole output (both visit the PCFs in the same
+    length order), and two row bands in caller order against the host entry
+    in caller order."""
     import torch
     import stablebear_gb300 as sb
     from stablebear_gb300 import _native as nat, synthetic
@@ -258,6 +260,11 @@ def test_device_entry_matches_host_entry():
                                             0, ctypes.c_void_p(st)))
     torch.cuda.synchronize()
     np.testing.assert_array_equal(out.cpu().numpy(), host)
+    sb.set_tuning(order=1)
+    try:
+        host = sb.pdist(arr(pts, off)).data
+    finally:
+        sb.set_tuning()
     # two bands written into separate buffers (row_begin a multiple of 512)
     cut = 512
     lo = torch.empty(cut * (cut - 1) // 2, dtype=torch.float32, device="cuda")
@@ -316,3 +323,46 @@ def test_invalid_input_raises_value_error():
                  sb.PcfArray([sb.Pcf(np.array([[0.0, 1.0]], dtype=np.float64))]))
     with pytest.raises(TypeError):
         sb.lp_distance(sb.Pcf(np.array([[0, 1], [1, 0]], dtype=np.int32)), sb.Pcf(np.array([[0, 0]], dtype=np.int32)))
+
+
+def test_device_length_order_is_the_stable_length_sort():
+    """The device entry's own processing order (computed on the GPU) gives
+    the same bits as passing the stable length sort as the permutation, for
+    pdist, the kernel matrix and cdist."""
+    import torch
+    from stablebear_gb300 import _native as nat, synthetic
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for n, lo, hi in ((3000, 1, 300), (37, 1, 9), (2049, 5, 6)):
+        pts, off = synthetic.gaussian(n, synthetic.uniform_lengths(lo, hi), np.float32, seed=n)
+        lens = np.diff(off.astype(np.int64))
+        perm = torch.from_numpy(np.argsort(lens, kind="stable").astype(np.uint32).view(np.int32)).cuda()
+        dp = torch.from_numpy(pts).cuda()
+        do = torch.from_numpy(off.astype(np.int64)).cuda()
+        lmax = int(lens.max())
+        for skip, op, p in ((nat.SKIP_LOWER_NODIAG, nat.OP_L1, 1.0), (nat.SKIP_LOWER, nat.OP_L2_INNER, 1.0)):
+            cnt = nat.lib().sbg_output_count(skip, n, n)
+            a = torch.empty(cnt, device="cuda")
+            b = torch.empty(cnt, device="cuda")
+            nat.check(nat.lib().sbg_pairwise_device(nat.F32, op, p, skip, dp.data_ptr(), do.data_ptr(), n, None, None,
+                                                    0, None, None, lmax, a.data_ptr(), 0, 0, 0, st))
+            nat.check(nat.lib().sbg_pairwise_device(nat.F32, op, p, skip, dp.data_ptr(), do.data_ptr(), n, None, None,
+                                                    0, perm.data_ptr(), None, lmax, b.data_ptr(), 0, 0, 0, st))
+            torch.cuda.synchronize()
+            assert torch.equal(a, b)
+        # cdist: rows and columns ordered separately
+        m = max(2, n // 3)
+        cp, co = pts[: int(off[m])], off[: m + 1]
+        cperm = torch.from_numpy(np.argsort(np.diff(co.astype(np.int64)), kind="stable").astype(np.uint32)
+                                 .view(np.int32)).cuda()
+        dcp = torch.from_numpy(np.ascontiguousarray(cp)).cuda()
+        dco = torch.from_numpy(co.astype(np.int64)).cuda()
+        a = torch.empty(n * m, device="cuda")
+        b = torch.empty(n * m, device="cuda")
+        nat.check(nat.lib().sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_NONE, dp.data_ptr(), do.data_ptr(),
+                                                n, dcp.data_ptr(), dco.data_ptr(), m, None, None, lmax, a.data_ptr(),
+                                                0, 0, 0, st))
+        nat.check(nat.lib().sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_NONE, dp.data_ptr(), do.data_ptr(),
+                                                n, dcp.data_ptr(), dco.data_ptr(), m, perm.data_ptr(),
+                                                cperm.data_ptr(), lmax, b.data_ptr(), 0, 0, 0, st))
+        torch.cuda.synchronize()
+        assert torch.equal(a, b)
