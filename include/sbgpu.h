@@ -308,6 +308,31 @@ int sbg_lp_norm_device(int dtype, double p, const void* points, const uint64_t* 
  * pairwise entries. */
 int sbg_lp_norm_host(int dtype, double p, const void* points, const uint64_t* offsets, uint64_t n, void* out);
 
+/* ---- barcodes to PCFs ---------------------------------------------------------- */
+
+/* kind: the summary a barcode is turned into. */
+#define SBG_STABLE_RANK 0 /* include/sbear/persistence/stable_rank.hpp:17-66 */
+#define SBG_BETTI_CURVE 1 /* include/sbear/persistence/betti_curve.hpp:21-84 */
+
+/* Upper bound on the points of the PCFs of n_barcodes barcodes holding
+ * n_bars bars in all: n_bars + n_barcodes (stable rank), 2 n_bars +
+ * n_barcodes (Betti curve). */
+uint64_t sbg_barcode_pcf_capacity(int kind, uint64_t n_barcodes, uint64_t n_bars);
+
+/* PCF of every barcode of a CSR of bars (interleaved (birth, death) pairs,
+ * bar_offsets[n_barcodes + 1]), as a PCF CSR: out_points (interleaved
+ * (t, v), room for out_capacity >= sbg_barcode_pcf_capacity points) and
+ * out_offsets[n_barcodes + 1].  Device pointers, caller's stream.  Replaces
+ * the reference's barcode_to_stable_rank / barcode_to_betti_curve tasks
+ * (PersistenceBarcodeSummary32/64 in src/python/persistence/
+ * py_barcode_summary.cpp), which convert one barcode at a time on the CPU. */
+int sbg_barcodes_to_pcfs_device(int kind, int dtype, const void* bars, const uint64_t* bar_offsets,
+                                uint64_t n_barcodes, uint64_t n_bars, void* out_points, uint64_t out_capacity,
+                                uint64_t* out_offsets, void* stream);
+/* The same from and to host memory, blocking. */
+int sbg_barcodes_to_pcfs_host(int kind, int dtype, const void* bars, const uint64_t* bar_offsets,
+                              uint64_t n_barcodes, void* out_points, uint64_t out_capacity, uint64_t* out_offsets);
+
 #ifdef __cplusplus
 }
 #endif

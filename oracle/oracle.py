@@ -59,6 +59,8 @@ def _load():
         lib.sbo_count_total_segments.restype = _U64
         lib.sbo_lp_norm.argtypes = [ctypes.c_int, ctypes.c_double, _P, _P, _U64, _P]
         lib.sbo_lp_norm.restype = ctypes.c_int
+        lib.sbo_barcodes_to_pcfs.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, _U64, _P, _P]
+        lib.sbo_barcodes_to_pcfs.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -309,3 +311,19 @@ def ref_lp_norm(points, offsets, p=1.0):
         a, b = int(off[i]), int(off[i + 1])
         out[i] = fn(_ptr(pts[a:b]), b - a, p)
     return out
+
+
+def barcodes_to_pcfs(bars, bar_offsets, kind):
+    """Stable rank (kind 0) or Betti curve (kind 1) PCFs of a CSR of bars
+    ((birth, death) rows), as (points, offsets): the restatement of the
+    reference's per-barcode loops."""
+    lib = _load()
+    bars = np.ascontiguousarray(bars)
+    boff = np.ascontiguousarray(bar_offsets, dtype=np.uint64)
+    n = len(boff) - 1
+    cap = (len(bars) if kind == 0 else 2 * len(bars)) + n
+    out = np.zeros((max(cap, 1), 2), dtype=bars.dtype)
+    ooff = np.zeros(n + 1, np.uint64)
+    rc = lib.sbo_barcodes_to_pcfs(kind, _dtype_code(bars), _ptr(bars), _ptr(boff), n, _ptr(out), _ptr(ooff))
+    assert rc == 0
+    return out[: int(ooff[-1])], ooff

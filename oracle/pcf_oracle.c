@@ -540,3 +540,97 @@ int sbo_lp_norm(int dtype, double p, const void* pts, const uint64_t* off, uint6
   }
   return 0;
 }
+
+/* ---------------------------------------------------------------------- */
+/* Barcodes to PCFs: the reference's loops, literally.                      */
+/*   barcode_to_stable_rank  include/sbear/persistence/stable_rank.hpp:17-66 */
+/*   barcode_to_betti_curve  include/sbear/persistence/betti_curve.hpp:21-84 */
+/* is_infinite: +inf or max (persistence/barcode.hpp:18-21).  The sorts are */
+/* qsort with the reference's orderings (lifetimes ascending; events by     */
+/* time, births before deaths at equal times).                              */
+/* ---------------------------------------------------------------------- */
+
+#define SBO_DEFINE_SUMMARY(T, SUF, TMAX)                                                   \
+  typedef struct { T time; int delta; } sbo_event_##SUF;                                   \
+  static int sbo_cmp_t_##SUF(const void* a, const void* b)                                 \
+  {                                                                                        \
+    T x = *(const T*)a, y = *(const T*)b;                                                  \
+    return (x < y) ? -1 : (y < x) ? 1 : 0;                                                 \
+  }                                                                                        \
+  static int sbo_cmp_ev_##SUF(const void* a, const void* b)                                \
+  {                                                                                        \
+    const sbo_event_##SUF* x = (const sbo_event_##SUF*)a;                                  \
+    const sbo_event_##SUF* y = (const sbo_event_##SUF*)b;                                  \
+    if (x->time < y->time || (x->time == y->time && x->delta > y->delta)) return -1;       \
+    if (y->time < x->time || (x->time == y->time && y->delta > x->delta)) return 1;        \
+    return 0;                                                                              \
+  }                                                                                        \
+  static int sbo_inf_##SUF(T v) { return v == (T)INFINITY || v == TMAX; }                  \
+  /* writes (t, v) pairs at out, returns the count */                                      \
+  static uint64_t sbo_stable_rank_one_##SUF(const T* bars, uint64_t m, T* out, T* tmp)     \
+  {                                                                                        \
+    uint64_t np = 0;                                                                       \
+    if (m == 0) { out[0] = 0; out[1] = 0; return 1; }                                      \
+    for (uint64_t k = 0; k < m; ++k) {                                                     \
+      T birth = bars[2 * k], death = bars[2 * k + 1];                                      \
+      tmp[k] = (death == TMAX) ? TMAX : death - birth;                                     \
+    }                                                                                      \
+    qsort(tmp, m, sizeof(T), sbo_cmp_t_##SUF);                                             \
+    T nAlive = (T)m;                                                                       \
+    out[2 * np] = 0; out[2 * np + 1] = nAlive; ++np;                                       \
+    T last = tmp[0];                                                                       \
+    for (uint64_t k = 0; k < m; ++k) {                                                     \
+      if (sbo_inf_##SUF(last)) break;                                                      \
+      if (tmp[k] != last) { out[2 * np] = last; out[2 * np + 1] = nAlive; ++np; last = tmp[k]; } \
+      nAlive -= 1;                                                                         \
+    }                                                                                      \
+    if (!sbo_inf_##SUF(last)) { out[2 * np] = last; out[2 * np + 1] = nAlive; ++np; }      \
+    return np;                                                                             \
+  }                                                                                        \
+  static uint64_t sbo_betti_one_##SUF(const T* bars, uint64_t m, T* out, sbo_event_##SUF* ev) \
+  {                                                                                        \
+    uint64_t ne = 0, np = 0;                                                               \
+    if (m == 0) { out[0] = 0; out[1] = 0; return 1; }                                      \
+    for (uint64_t k = 0; k < m; ++k) {                                                     \
+      ev[ne].time = bars[2 * k]; ev[ne].delta = 1; ++ne;                                   \
+      if (!sbo_inf_##SUF(bars[2 * k + 1])) { ev[ne].time = bars[2 * k + 1]; ev[ne].delta = -1; ++ne; } \
+    }                                                                                      \
+    qsort(ev, ne, sizeof(sbo_event_##SUF), sbo_cmp_ev_##SUF);                              \
+    T count = 0, lastTime = 0;                                                             \
+    for (uint64_t k = 0; k < ne; ++k) {                                                    \
+      if (ev[k].time != lastTime) { out[2 * np] = lastTime; out[2 * np + 1] = count; ++np; lastTime = ev[k].time; } \
+      count += (T)ev[k].delta;                                                             \
+    }                                                                                      \
+    out[2 * np] = lastTime; out[2 * np + 1] = count; ++np;                                 \
+    return np;                                                                             \
+  }
+
+SBO_DEFINE_SUMMARY(float, f32, FLT_MAX)
+SBO_DEFINE_SUMMARY(double, f64, DBL_MAX)
+
+/* kind 0 stable rank, 1 Betti curve.  out has room for the bound (m + 1 or
+ * 2 m + 1 points per barcode); out_off[n + 1] receives the PCF offsets. */
+int sbo_barcodes_to_pcfs(int kind, int dtype, const void* bars, const uint64_t* boff, uint64_t n, void* out,
+                         uint64_t* out_off)
+{
+  uint64_t mmax = 0;
+  for (uint64_t i = 0; i < n; ++i) if (boff[i + 1] - boff[i] > mmax) mmax = boff[i + 1] - boff[i];
+  void* tmp = malloc((2 * mmax + 1) * 16);
+  if (!tmp) return -1;
+  out_off[0] = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t m = boff[i + 1] - boff[i], np;
+    if (dtype == 0) {
+      const float* b = (const float*)bars + 2 * boff[i];
+      float* o = (float*)out + 2 * out_off[i];
+      np = kind == 0 ? sbo_stable_rank_one_f32(b, m, o, (float*)tmp) : sbo_betti_one_f32(b, m, o, (sbo_event_f32*)tmp);
+    } else {
+      const double* b = (const double*)bars + 2 * boff[i];
+      double* o = (double*)out + 2 * out_off[i];
+      np = kind == 0 ? sbo_stable_rank_one_f64(b, m, o, (double*)tmp) : sbo_betti_one_f64(b, m, o, (sbo_event_f64*)tmp);
+    }
+    out_off[i + 1] = out_off[i] + np;
+  }
+  free(tmp);
+  return 0;
+}

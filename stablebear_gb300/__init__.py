@@ -20,6 +20,7 @@ from .system import (
 from .task import StoppableTask, EmptyTask
 from .io import save, load
 from .norms import lp_norm, Norms_f32_f32, Norms_f64_f64
+from . import persistence
 
 __all__ = [
     "Pcf", "PcfArray", "pcf32", "pcf64", "pcf32i", "pcf64i", "float32", "float64", "zeros",
@@ -29,6 +30,7 @@ __all__ = [
     "force_cpu", "set_block_size", "limit_cpus", "limit_gpus", "set_cuda_threshold", "get_cuda_threshold",
     "set_device_verbose", "set_min_block_side", "set_tuning", "build_type", "get_ngpus",
     "StoppableTask", "EmptyTask", "save", "load", "lp_norm", "Norms_f32_f32", "Norms_f64_f64",
+    "persistence",
 ]
 
 __version__ = "0.1.0"

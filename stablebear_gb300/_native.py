@@ -82,6 +82,9 @@ SIGNATURES = {
     "sbg_dense_to_condensed_device": (_I, [_I, _I, _U64, _P, _U64, _P, _P, _P]),
     "sbg_lp_norm_device": (_I, [_I, _D, _P, _P, _U64, _P, _P]),
     "sbg_lp_norm_host": (_I, [_I, _D, _P, _P, _U64, _P]),
+    "sbg_barcode_pcf_capacity": (_U64, [_I, _U64, _U64]),
+    "sbg_barcodes_to_pcfs_device": (_I, [_I, _I, _P, _P, _U64, _U64, _P, _U64, _P, _P]),
+    "sbg_barcodes_to_pcfs_host": (_I, [_I, _I, _P, _P, _U64, _P, _U64, _P]),
 }
 
 _lib = None

@@ -230,3 +230,37 @@ def test_norm_known_answers():
     assert one([[0, 0]], 2.0) == 0.0
     # repeated t = 0: the walk starts at the last breakpoint with t <= 0
     assert one([[0, 7], [0, 1], [2, 0]], 1.0) == 2.0
+
+
+# ---- barcodes to PCFs ------------------------------------------------------------
+
+def _summary(bars, kind, dt=np.float64):
+    b = np.array(bars, dt).reshape(-1, 2)
+    pts, off = orc.barcodes_to_pcfs(b, np.array([0, len(b)], np.uint64), kind)
+    return pts.tolist()
+
+
+def test_stable_rank_known_answers():
+    """test/python/persistence/test_stable_rank.py and
+    test/test_barcode_and_stable_rank.cpp, restated."""
+    for dt in (np.float32, np.float64):
+        assert _summary([], 0, dt) == [[0, 0]]
+        assert _summary([[0, 1], [0, 2], [0, 3]], 0, dt) == [[0, 3], [1, 2], [2, 1], [3, 0]]
+        assert _summary([[0, 1], [0, 3], [0, 2], [0, 2], [1, 3]], 0, dt) == [[0, 5], [1, 4], [2, 1], [3, 0]]
+        assert _summary([[0, 1], [0, 3], [0, 2], [0, np.inf], [1, 3]], 0, dt) == [[0, 5], [1, 4], [2, 2], [3, 1]]
+        assert _summary([[0, 1], [0, 2]], 0, dt) == [[0, 2], [1, 1], [2, 0]]
+        # a death at the dtype's maximum is infinite too
+        assert _summary([[0, np.finfo(dt).max], [0, 1]], 0, dt) == [[0, 2], [1, 1]]
+        # all bars infinite: only the first point
+        assert _summary([[0, np.inf], [1, np.inf]], 0, dt) == [[0, 2]]
+
+
+def test_betti_curve_known_answers():
+    """test/python/persistence/test_betti_curve.py, restated."""
+    for dt in (np.float32, np.float64):
+        assert _summary([], 1, dt) == [[0, 0]]
+        assert _summary([[0, 2]], 1, dt) == [[0, 1], [2, 0]]
+        assert _summary([[1, 3]], 1, dt) == [[0, 0], [1, 1], [3, 0]]
+        assert _summary([[0, 2], [1, 3], [0.5, 1.5]], 1, dt) == [[0, 1], [0.5, 2], [1, 3], [1.5, 2], [2, 1], [3, 0]]
+        assert _summary([[0, 1], [0, 2], [0, 3]], 1, dt) == [[0, 3], [1, 2], [2, 1], [3, 0]]
+        assert _summary([[0, np.inf], [1, 2]], 1, dt) == [[0, 1], [1, 2], [2, 1]]
