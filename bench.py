@@ -421,11 +421,13 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    launches0 = lib.sbg_kernel_launches()
     evs[0].record(stream)
     for k in range(args.steps):
         step()
         evs[k + 1].record(stream)
     torch.cuda.synchronize()
+    launches = int(lib.sbg_kernel_launches() - launches0)
     if dist:
         dist.barrier()
     clk = clocks.stop()
@@ -516,7 +518,7 @@ def main():
                      "frac": achieved / peak["value"], "traffic": traffic, "peak_source": peak["source"],
                      "work_model": f"{W_SEG} FP32 lane-ops per merged segment x {segs} segments per launch"},
         "hbm_output_stream": {"bytes_per_launch": pairs * 4, "achieved_gbs": pairs * 4 / (ms_step / 1e3) / 1e9},
-        "clocks": clk, "gpu_launches": args.steps, "step_ms": per,
+        "clocks": clk, "gpu_launches": launches, "step_ms": per,
     }
     if cpu:
         line["cpu_baseline"] = cpu

@@ -267,6 +267,12 @@ int sbg_pairwise_device_noalloc(int dtype, int op, double p, int skip_mode,
                                 void* out, uint64_t out_base, uint64_t row_begin, uint64_t row_end,
                                 void* stream);
 
+/* Kernels this library has launched in this process so far (all threads and
+ * devices; a CUDA graph replay counts the kernels it holds).  Read it before
+ * and after a region to count the region's launches.  No counterpart in the
+ * reference. */
+uint64_t sbg_kernel_launches(void);
+
 /* Number of output elements of a problem (n(n-1)/2, n(n+1)/2 or n_rows*n_cols). */
 uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols);
 

@@ -277,14 +277,14 @@ namespace sbg
       SBG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms);
       fn<<<grid, warps * 32, smem, st>>>(B);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
     }
     if (bop == BWD_INNER)
     {
       // after the pair kernel on the same stream: plain adds are race-free
       const unsigned blocks = (unsigned)std::min<uint64_t>((n + 7) / 8, (uint64_t)dev.sms * 8);
       diag_backward_kernel<T><<<blocks, 256, 0, st>>>(B.pk, off, n, npts, grad_out, grad);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
     }
   }
 }

@@ -47,6 +47,7 @@ namespace sbg
     uint64_t total_items = 0, total_pairs = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    uint64_t graph_kernels = 0;  // kernels one replay of the graph runs
 
     ~Batch() override { drop_graph(); }
 
@@ -103,7 +104,11 @@ namespace sbg
         cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess)
         {
+          // kernels recorded during capture have not run: count them per replay
+          const uint64_t before = kernel_launches();
           try { enqueue(cap); } catch (...) { cudaGraph_t g0; cudaStreamEndCapture(cap, &g0); if (g0) cudaGraphDestroy(g0); cudaStreamDestroy(cap); throw; }
+          graph_kernels = kernel_launches() - before;
+          uncount_launches(graph_kernels);
           e = cudaStreamEndCapture(cap, &graph);
         }
         cudaStreamDestroy(cap);
@@ -111,6 +116,7 @@ namespace sbg
         SBG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
       }
       SBG_CUDA(cudaGraphLaunch(exec, st));
+      count_launches(graph_kernels);
     }
 
     double time_once(cudaStream_t st, int reps)

@@ -251,6 +251,8 @@ extern "C"
     return n;
   }
 
+  uint64_t sbg_kernel_launches(void) { return kernel_launches(); }
+
   uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols)
   {
     return output_count(skip_mode, n_rows, n_cols);

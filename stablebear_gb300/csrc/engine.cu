@@ -42,6 +42,19 @@ namespace sbg
     throw Error(st, msg);
   }
 
+  static std::atomic<uint64_t> g_kernel_launches{0};
+
+  cudaError_t launched()
+  {
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+    return cudaGetLastError();
+  }
+
+  void count_launches(uint64_t n) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
+  void uncount_launches(uint64_t n) { g_kernel_launches.fetch_sub(n, std::memory_order_relaxed); }
+
+  uint64_t kernel_launches() { return g_kernel_launches.load(std::memory_order_relaxed); }
+
   Settings& settings()
   {
     static Settings s;
@@ -312,7 +325,7 @@ namespace sbg
     unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)dev.sms * 4);
     if (blocks == 0) blocks = 1;
     max_len_kernel<<<blocks, 256, 0, st>>>(off, n, (unsigned int*)buf.p);
-    SBG_CUDA(cudaGetLastError());
+    SBG_CUDA(launched());
     unsigned int h = 0;
     SBG_CUDA(cudaMemcpyAsync(&h, buf.p, sizeof(h), cudaMemcpyDeviceToHost, st));
     SBG_CUDA(cudaStreamSynchronize(st));

@@ -73,47 +73,57 @@ namespace sbg
       }
     };
 
+    // Two tiles per CTA iteration, both loaded before the barrier, so each
+    // thread keeps eight loads in flight.
     template <typename T>
     __global__ void __launch_bounds__(TILE * ROWS) condensed_to_dense_kernel(
         const T* __restrict__ cond, uint64_t n, bool diag, T* __restrict__ dense, uint64_t ld,
         uint64_t row_begin, uint64_t row_end, TileSet ts)
     {
-      __shared__ T tile[TILE][TILE + 1];
+      __shared__ T tile[2][TILE][TILE + 1];
       const int tx = threadIdx.x, ty = threadIdx.y;
-      for (uint64_t k = blockIdx.x; k < ts.count; k += gridDim.x)
+      for (uint64_t k0 = 2ull * blockIdx.x; k0 < ts.count; k0 += 2ull * gridDim.x)
       {
-        uint64_t a, b;
-        ts.decode(k, &a, &b);
-        const uint64_t i0 = a * TILE, j0 = b * TILE;
-        // Lower tile (a, b): row i = i0 + r, column j = j0 + tx.
-        const uint64_t j = j0 + tx;
+        uint64_t a[2], b[2];
+        const int nt = k0 + 1 < ts.count ? 2 : 1;
+        T v[2][TILE / ROWS];
 #pragma unroll
-        for (int r = ty; r < TILE; r += ROWS)
+        for (int u = 0; u < 2; ++u)
         {
-          const uint64_t i = i0 + r;
-          T v = T(0);
-          if (i < n && j < n && (j < i || (diag && j == i))) v = cond[cond_index(diag, i, j)];
-          tile[r][tx] = v;
-        }
-        __syncthreads();
-        // Dense tile (a, b): rows of block a inside the band.
-        for (int r = ty; r < TILE; r += ROWS)
-        {
-          const uint64_t i = i0 + r, j = j0 + tx;
-          if (i >= row_begin && i < row_end && j < n)
+          if (u < nt) ts.decode(k0 + u, &a[u], &b[u]);
+          else { a[u] = 0; b[u] = 0; }
+          const uint64_t i0 = a[u] * TILE, j = b[u] * TILE + tx;
+#pragma unroll
+          for (int q = 0; q < TILE / ROWS; ++q)
           {
-            // on the diagonal tile the upper half comes from the transposed lower half
-            const T v = (a != b || tx <= r) ? tile[r][tx] : tile[tx][r];
-            dense[(i - row_begin) * ld + j] = v;
+            const uint64_t i = i0 + ty + q * ROWS;
+            v[u][q] = (u < nt && i < n && j < n && (j < i || (diag && j == i))) ? cond[cond_index(diag, i, j)] : T(0);
           }
         }
-        // Dense tile (b, a), a > b: the transpose.
-        if (a != b)
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+          for (int q = 0; q < TILE / ROWS; ++q) tile[u][ty + q * ROWS][tx] = v[u][q];
+        __syncthreads();
+        for (int u = 0; u < nt; ++u)
         {
+          const uint64_t i0 = a[u] * TILE, j0 = b[u] * TILE;
+          // dense tile (a, b): rows of block a inside the band; on the
+          // diagonal tile the upper half is the transposed lower half
           for (int r = ty; r < TILE; r += ROWS)
           {
-            const uint64_t i = j0 + r, j = i0 + tx;
-            if (i >= row_begin && i < row_end && j < n) dense[(i - row_begin) * ld + j] = tile[tx][r];
+            const uint64_t i = i0 + r, j = j0 + tx;
+            if (i >= row_begin && i < row_end && j < n)
+              dense[(i - row_begin) * ld + j] = (a[u] != b[u] || tx <= r) ? tile[u][r][tx] : tile[u][tx][r];
+          }
+          // dense tile (b, a), a > b: the transpose
+          if (a[u] != b[u])
+          {
+            for (int r = ty; r < TILE; r += ROWS)
+            {
+              const uint64_t i = j0 + r, j = i0 + tx;
+              if (i >= row_begin && i < row_end && j < n) dense[(i - row_begin) * ld + j] = tile[u][tx][r];
+            }
           }
         }
         __syncthreads();
@@ -135,19 +145,27 @@ namespace sbg
         uint64_t a, b;
         ts.decode(k, &a, &b);
         const uint64_t i0 = a * TILE, j0 = b * TILE;
-        // The mirror tile (b, a), read coalesced and kept transposed.
-        for (int r = ty; r < TILE; r += ROWS)
+        // The mirror tile (b, a), read coalesced and kept transposed, and
+        // this thread's values of the lower tile, all loads before the barrier.
+        T low[TILE / ROWS];
+#pragma unroll
+        for (int q = 0; q < TILE / ROWS; ++q)
         {
+          const int r = ty + q * ROWS;
           const uint64_t i = j0 + r, j = i0 + tx;
           upper[tx][r] = (i < n && j < n) ? dense[i * ld + j] : T(0);
+          const uint64_t li = i0 + r, lj = j0 + tx;
+          low[q] = (li < n && lj < n && lj <= li) ? dense[li * ld + lj] : T(0);
         }
         __syncthreads();
-        for (int r = ty; r < TILE; r += ROWS)
+#pragma unroll
+        for (int q = 0; q < TILE / ROWS; ++q)
         {
+          const int r = ty + q * ROWS;
           const uint64_t i = i0 + r, j = j0 + tx;
           if (i < n && j < n && j <= i)
           {
-            const T v = dense[i * ld + j];
+            const T v = low[q];
             if (!(v == upper[r][tx])) f |= 1u;  // NaN counts as asymmetric, as != does in the reference
             if (j == i)
             {
@@ -171,6 +189,7 @@ namespace sbg
     {
       const DeviceInfo d = device_info();
       const uint64_t g = (uint64_t)d.sms * 8;  // 8 CTAs of 256 threads per SM
+      tiles = (tiles + 1) / 2;                  // condensed_to_dense takes two tiles per iteration
       return (int)(tiles < g ? (tiles ? tiles : 1) : g);
     }
 
@@ -232,7 +251,7 @@ extern "C"
       else
         condensed_to_dense_kernel<double><<<grid, block, 0, st>>>((const double*)condensed, n, diag, (double*)dense,
                                                                    ld, row_begin, row_end, ts);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
     });
   }
 
@@ -259,7 +278,7 @@ extern "C"
       else
         dense_to_condensed_kernel<double><<<grid, block, 0, st>>>((const double*)dense, n, ld, diag,
                                                                    (double*)condensed, flags, ts);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
     });
   }
 }

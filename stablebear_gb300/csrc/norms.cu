@@ -83,7 +83,7 @@ namespace sbg
       const uint64_t threads = n * 32;
       const unsigned grid = (unsigned)ceil_div_u64(threads, 256);
       lp_norm_kernel<T><<<grid, 256, 0, st>>>((const T*)pts, off, n, (T)p, p == 1.0, (T*)out);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
     }
 
     void check_norm_args(int dtype, double p)

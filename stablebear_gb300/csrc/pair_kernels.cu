@@ -611,7 +611,7 @@ namespace sbg
       if (e != cudaSuccess) return e;
     }
     fn<<<grid, block, smem, s>>>(L);
-    return cudaGetLastError();
+    return launched();
   }
 
   template <typename T>
@@ -630,7 +630,7 @@ namespace sbg
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     fn<<<grid, block, smem, s>>>(L);
-    return cudaGetLastError();
+    return launched();
   }
 
   template <typename T>
@@ -654,7 +654,7 @@ namespace sbg
     const uint64_t max_blocks = (uint64_t)sms * 8;
     if (blocks > max_blocks) blocks = max_blocks;
     pack_segments_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(pts, off, n, out, cap);
-    return cudaGetLastError();
+    return launched();
   }
 
   template cudaError_t launch_pairs<float>(const LaunchParams<float>&, int, int, int, int, size_t, cudaStream_t);

@@ -33,10 +33,13 @@ namespace sbg
     SBG_CUDA(cudaEventCreate(&e0));
     SBG_CUDA(cudaEventCreate(&e1));
     for (int w = 0; w < 2; ++w) fma_rate_kernel<T, ITERS><<<blocks, 256>>>(T(1), sink.as<T>());
-    SBG_CUDA(cudaGetLastError());
+    SBG_CUDA(launched());
+    count_launches(1);
     SBG_CUDA(cudaEventRecord(e0));
     const int reps = 5;
     for (int r = 0; r < reps; ++r) fma_rate_kernel<T, ITERS><<<blocks, 256>>>(T(1), sink.as<T>());
+    SBG_CUDA(launched());
+    count_launches(reps - 1);
     SBG_CUDA(cudaEventRecord(e1));
     SBG_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;

@@ -363,16 +363,16 @@ namespace sbg
       const unsigned grid = (unsigned)std::min<uint64_t>(n, (uint64_t)dev.sms * 8);
       barcode_summary_kernel<T, KIND><<<grid, PB_THREADS, 0, st>>>(bars, boff, n, (PKey<T>*)scratch.p, (T*)padded.p,
                                                                    (uint32_t*)counts.p);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
       scan_block_sums_kernel<<<(unsigned)nb, SCAN_BLOCK, 0, st>>>((const uint32_t*)counts.p, n, (uint64_t*)sums.p);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
       scan_sums_kernel<<<1, 32, 0, st>>>((uint64_t*)sums.p, nb);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
       scan_finish_kernel<<<(unsigned)nb, SCAN_BLOCK, 0, st>>>((const uint32_t*)counts.p, n, (const uint64_t*)sums.p,
                                                               out_off);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
       pack_points_kernel<T, KIND><<<grid, 128, 0, st>>>((const T*)padded.p, boff, n, out_off, out, out_capacity);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
     }
 
     void check_summary_args(int kind, int dtype)

@@ -104,17 +104,17 @@ namespace sbg
     const unsigned tiles = (unsigned)(npad / tile);
     // every stage that fits in a tile
     tile_stages_kernel<<<tiles, SORT_THREADS, 0, st>>>(keys, npad, tile, 2, tile, tile / 2);
-    SBG_CUDA(cudaGetLastError());
+    SBG_CUDA(launched());
     for (uint64_t k = 2 * tile; k <= npad; k <<= 1)
     {
       for (uint64_t j = k / 2; j >= tile; j >>= 1)
       {
         const uint64_t pairs = npad / 2;
         global_step_kernel<<<(unsigned)((pairs + 255) / 256), 256, 0, st>>>(keys, npad, j, k);
-        SBG_CUDA(cudaGetLastError());
+        SBG_CUDA(launched());
       }
       tile_stages_kernel<<<tiles, SORT_THREADS, 0, st>>>(keys, npad, tile, k, k, tile / 2);
-      SBG_CUDA(cudaGetLastError());
+      SBG_CUDA(launched());
     }
   }
 
@@ -134,9 +134,9 @@ namespace sbg
     uint64_t* keys = static_cast<uint64_t*>(scratch);
     const unsigned blocks = (unsigned)std::min<uint64_t>((npad + 255) / 256, 4096);
     make_keys_kernel<<<blocks, 256, 0, st>>>(off, n, npad, keys);
-    SBG_CUDA(cudaGetLastError());
+    SBG_CUDA(launched());
     sort_keys_u64(keys, npad, st);
     keys_to_perm_kernel<<<blocks, 256, 0, st>>>(keys, n, perm);
-    SBG_CUDA(cudaGetLastError());
+    SBG_CUDA(launched());
   }
 }

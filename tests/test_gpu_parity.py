@@ -366,3 +366,33 @@ def test_device_length_order_is_the_stable_length_sort():
                                                 cperm.data_ptr(), lmax, b.data_ptr(), 0, 0, 0, st))
         torch.cuda.synchronize()
         assert torch.equal(a, b)
+
+
+def test_kernel_launch_counter():
+    """sbg_kernel_launches counts the kernels of a call: one pair kernel in
+    caller order; the length order adds its sort kernels."""
+    import torch
+    import stablebear_gb300 as sb
+    from stablebear_gb300 import _native as nat, synthetic
+    lib = nat.lib()
+    pts, off = synthetic.plain_l1(600, seed=2)
+    dp = torch.from_numpy(pts).cuda()
+    do = torch.from_numpy(off.astype(np.int64)).cuda()
+    n = len(off) - 1
+    out = torch.empty(n * (n - 1) // 2, device="cuda")
+    lmax = int(np.diff(off.astype(np.int64)).max())
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def call():
+        before = lib.sbg_kernel_launches()
+        nat.check(lib.sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                          do.data_ptr(), n, None, None, 0, None, None, lmax, out.data_ptr(), 0, 0, 0,
+                                          st))
+        return lib.sbg_kernel_launches() - before
+
+    sb.set_tuning(order=1)
+    try:
+        assert call() == 1
+    finally:
+        sb.set_tuning()
+    assert call() > 1
