@@ -271,13 +271,19 @@ namespace sbg
     return s;
   }
 
+  // The host version of the windowed length order (sort.cu); both give the
+  // same permutation.
   static std::vector<uint32_t> length_order(const uint64_t* off, uint64_t n)
   {
     std::vector<uint32_t> perm(n);
     std::iota(perm.begin(), perm.end(), 0u);
-    std::stable_sort(perm.begin(), perm.end(), [off](uint32_t a, uint32_t b) {
-      return (off[a + 1] - off[a]) < (off[b + 1] - off[b]);
-    });
+    auto len = [off](uint32_t a) { return std::min<uint64_t>(off[a + 1] - off[a], 0xffffffffull); };
+    for (uint64_t w0 = 0; w0 < n; w0 += LENGTH_ORDER_WINDOW)
+    {
+      const uint64_t w1 = std::min<uint64_t>(n, w0 + LENGTH_ORDER_WINDOW);
+      std::stable_sort(perm.begin() + w0, perm.begin() + w1,
+                       [&len](uint32_t a, uint32_t b) { return len(a) < len(b); });
+    }
     return perm;
   }
 

@@ -197,9 +197,10 @@ namespace sbg
   uint64_t output_count(int mode, uint64_t n_rows, uint64_t n_cols);
   uint64_t row_output_start(int mode, uint64_t row, uint64_t n_cols);
 
-  // Device-side length order (sort.cu): perm[i] = index of the PCF with the
-  // i-th smallest breakpoint count, ties by index.  `scratch` holds
-  // length_order_scratch_bytes(n) bytes.
+  // Length order (sort.cu): within each window of LENGTH_ORDER_WINDOW
+  // consecutive PCFs, by breakpoint count, ties by index.  The device
+  // version; `scratch` holds length_order_scratch_bytes(n) bytes.
+  constexpr uint64_t LENGTH_ORDER_WINDOW = 1024;
   uint64_t length_order_scratch_bytes(uint64_t n);
   void length_order_device(const uint64_t* off, uint64_t n, uint32_t* perm, void* scratch, cudaStream_t st);
   // Ascending bitonic sort of npad (a power of two) 64-bit keys in place.

@@ -1,11 +1,17 @@
-// Length order of a PCF set on the device: the permutation that visits PCFs
-// by increasing breakpoint count, ties by index (the same permutation as a
-// stable host sort by length).  Grouping columns of similar length keeps the
-// warp-uniform step count of the pair kernels close to the work each lane
-// does; the order is computed on the stream, with no host round trip.
+// Length order of a PCF set on the device: within each window of
+// LENGTH_ORDER_WINDOW consecutive PCFs, the PCFs by increasing breakpoint
+// count, ties by index (the same permutation as a stable host sort of each
+// window).  Grouping columns of similar length keeps the warp-uniform step
+// count of the pair kernels close to the work each lane does.  Sorting only
+// within windows keeps the output locality: the 32 results of a warp land in
+// one window of a condensed row, which the CTAs working on neighbouring
+// column groups fill at the same time, so L2 writes whole sectors back (a
+// global sort scatters every store and multiplied DRAM traffic ~9x).  The
+// order is computed on the stream, with no host round trip.
 //
-// Keys (length << 32 | index) are unique, so a bitonic network (not stable
-// by itself) gives the one deterministic order.  The key array is padded to
+// Keys (window << 42 | min(length, 2^32 - 1) << 10 | index in window) are
+// unique, so a bitonic network (not stable by itself) gives the one
+// deterministic order.  The key array is padded to
 // a power of two with all-ones keys, which sort last.  Sorting network:
 // tiles of 2048 keys are sorted in shared memory; stages whose partner
 // distance is a tile or more run as one global compare-exchange pass each,
@@ -83,7 +89,7 @@ namespace sbg
         {
           uint64_t len = off[i + 1] - off[i];
           if (len > 0xffffffffull) len = 0xffffffffull;
-          keys[i] = (len << 32) | i;
+          keys[i] = ((i >> 10) << 42) | (len << 10) | (i & 1023);
         }
         else keys[i] = ~0ull;
       }
@@ -92,7 +98,7 @@ namespace sbg
     __global__ void keys_to_perm_kernel(const uint64_t* __restrict__ keys, uint64_t n, uint32_t* __restrict__ perm)
     {
       for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        perm[i] = (uint32_t)(keys[i] & 0xffffffffull);
+        perm[i] = (uint32_t)(((keys[i] >> 42) << 10) | (keys[i] & 1023));
     }
   }
 
@@ -118,24 +124,37 @@ namespace sbg
     }
   }
 
-  uint64_t length_order_scratch_bytes(uint64_t n)
+  static_assert(LENGTH_ORDER_WINDOW == 1024, "the key layout holds 10 bits of index within a window");
+  static_assert(LENGTH_ORDER_WINDOW <= SORT_TILE, "a window is sorted inside one tile");
+
+  // Keys padded to whole windows (or, below one window, to a power of two).
+  static uint64_t padded_keys(uint64_t n)
   {
+    if (n >= LENGTH_ORDER_WINDOW) return (n + LENGTH_ORDER_WINDOW - 1) / LENGTH_ORDER_WINDOW * LENGTH_ORDER_WINDOW;
     uint64_t npad = 1;
     while (npad < n) npad <<= 1;
-    return npad * sizeof(uint64_t);
+    return npad;
   }
+
+  uint64_t length_order_scratch_bytes(uint64_t n) { return padded_keys(n) * sizeof(uint64_t); }
 
   void length_order_device(const uint64_t* off, uint64_t n, uint32_t* perm, void* scratch, cudaStream_t st)
   {
     if (n == 0) return;
     if (n > 0xffffffffull) throw Error(ST_INVALID_ARGUMENT, "too many PCFs for a 32-bit processing order");
-    uint64_t npad = 1;
-    while (npad < n) npad <<= 1;
+    const uint64_t npad = padded_keys(n);
     uint64_t* keys = static_cast<uint64_t*>(scratch);
     const unsigned blocks = (unsigned)std::min<uint64_t>((npad + 255) / 256, 4096);
     make_keys_kernel<<<blocks, 256, 0, st>>>(off, n, npad, keys);
     SBG_CUDA(launched());
-    sort_keys_u64(keys, npad, st);
+    // The window sits in the keys' high bits, so sorting every window on its
+    // own (one tile each) is the whole sort.
+    const uint64_t tile = npad < LENGTH_ORDER_WINDOW ? npad : LENGTH_ORDER_WINDOW;
+    if (tile >= 2)
+    {
+      tile_stages_kernel<<<(unsigned)(npad / tile), SORT_THREADS, 0, st>>>(keys, npad, tile, 2, tile, tile / 2);
+      SBG_CUDA(launched());
+    }
     keys_to_perm_kernel<<<blocks, 256, 0, st>>>(keys, n, perm);
     SBG_CUDA(launched());
   }

@@ -325,17 +325,22 @@ def test_invalid_input_raises_value_error():
         sb.lp_distance(sb.Pcf(np.array([[0, 1], [1, 0]], dtype=np.int32)), sb.Pcf(np.array([[0, 0]], dtype=np.int32)))
 
 
+def _window_order(lens, w=1024):
+    """Stable sort by length inside each window of w consecutive PCFs."""
+    return np.concatenate([k + np.argsort(lens[k:k + w], kind="stable") for k in range(0, len(lens), w)])
+
+
 def test_device_length_order_is_the_stable_length_sort():
     """The device entry's own processing order (computed on the GPU) gives
-    the same bits as passing the stable length sort as the permutation, for
-    pdist, the kernel matrix and cdist."""
+    the same bits as passing the windowed stable length sort as the
+    permutation, for pdist, the kernel matrix and cdist."""
     import torch
     from stablebear_gb300 import _native as nat, synthetic
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for n, lo, hi in ((3000, 1, 300), (37, 1, 9), (2049, 5, 6)):
         pts, off = synthetic.gaussian(n, synthetic.uniform_lengths(lo, hi), np.float32, seed=n)
         lens = np.diff(off.astype(np.int64))
-        perm = torch.from_numpy(np.argsort(lens, kind="stable").astype(np.uint32).view(np.int32)).cuda()
+        perm = torch.from_numpy(_window_order(lens).astype(np.uint32).view(np.int32)).cuda()
         dp = torch.from_numpy(pts).cuda()
         do = torch.from_numpy(off.astype(np.int64)).cuda()
         lmax = int(lens.max())
@@ -352,7 +357,7 @@ def test_device_length_order_is_the_stable_length_sort():
         # cdist: rows and columns ordered separately
         m = max(2, n // 3)
         cp, co = pts[: int(off[m])], off[: m + 1]
-        cperm = torch.from_numpy(np.argsort(np.diff(co.astype(np.int64)), kind="stable").astype(np.uint32)
+        cperm = torch.from_numpy(_window_order(np.diff(co.astype(np.int64))).astype(np.uint32)
                                  .view(np.int32)).cuda()
         dcp = torch.from_numpy(np.ascontiguousarray(cp)).cuda()
         dco = torch.from_numpy(co.astype(np.int64)).cuda()
