@@ -203,8 +203,6 @@ namespace sbg
   constexpr uint64_t LENGTH_ORDER_WINDOW = 1024;
   uint64_t length_order_scratch_bytes(uint64_t n);
   void length_order_device(const uint64_t* off, uint64_t n, uint32_t* perm, void* scratch, cudaStream_t st);
-  // Ascending bitonic sort of npad (a power of two) 64-bit keys in place.
-  void sort_keys_u64(uint64_t* keys, uint64_t npad, cudaStream_t st);
 
   // Launch accounting: every kernel launch of the library is followed by
   // launched(), which counts it and returns the launch error.  A CUDA graph

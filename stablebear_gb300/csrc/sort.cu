@@ -11,11 +11,8 @@
 //
 // Keys (window << 42 | min(length, 2^32 - 1) << 10 | index in window) are
 // unique, so a bitonic network (not stable by itself) gives the one
-// deterministic order.  The key array is padded to
-// a power of two with all-ones keys, which sort last.  Sorting network:
-// tiles of 2048 keys are sorted in shared memory; stages whose partner
-// distance is a tile or more run as one global compare-exchange pass each,
-// and the rest of every stage finishes inside the tiles again.
+// deterministic order.  Each window is sorted by one CTA in shared memory;
+// the last window is padded with all-ones keys, which sort last.
 #include "sbg_internal.hpp"
 
 #include <algorithm>
@@ -65,21 +62,6 @@ namespace sbg
       (void)n;
     }
 
-    // One compare-exchange pass of stage k at partner distance j over the
-    // whole array (n / 2 pairs).
-    __global__ void global_step_kernel(uint64_t* keys, uint64_t n, uint64_t j, uint64_t k)
-    {
-      const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-      if (t >= n / 2) return;
-      const uint64_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));  // j is a power of two
-      uint64_t a = keys[i], b = keys[i + j];
-      if ((a > b) == ((i & k) == 0))
-      {
-        keys[i] = b;
-        keys[i + j] = a;
-      }
-    }
-
     __global__ void make_keys_kernel(const uint64_t* __restrict__ off, uint64_t n, uint64_t npad,
                                      uint64_t* __restrict__ keys)
     {
@@ -99,28 +81,6 @@ namespace sbg
     {
       for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
         perm[i] = (uint32_t)(((keys[i] >> 42) << 10) | (keys[i] & 1023));
-    }
-  }
-
-  void sort_keys_u64(uint64_t* keys, uint64_t npad, cudaStream_t st)
-  {
-    if (npad < 2) return;
-    if ((npad & (npad - 1)) != 0) throw Error(ST_INTERNAL, "sort_keys_u64: length must be a power of two");
-    const uint64_t tile = npad < SORT_TILE ? npad : SORT_TILE;
-    const unsigned tiles = (unsigned)(npad / tile);
-    // every stage that fits in a tile
-    tile_stages_kernel<<<tiles, SORT_THREADS, 0, st>>>(keys, npad, tile, 2, tile, tile / 2);
-    SBG_CUDA(launched());
-    for (uint64_t k = 2 * tile; k <= npad; k <<= 1)
-    {
-      for (uint64_t j = k / 2; j >= tile; j >>= 1)
-      {
-        const uint64_t pairs = npad / 2;
-        global_step_kernel<<<(unsigned)((pairs + 255) / 256), 256, 0, st>>>(keys, npad, j, k);
-        SBG_CUDA(launched());
-      }
-      tile_stages_kernel<<<tiles, SORT_THREADS, 0, st>>>(keys, npad, tile, k, k, tile / 2);
-      SBG_CUDA(launched());
     }
   }
 
