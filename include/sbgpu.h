@@ -267,6 +267,13 @@ int sbg_pairwise_device_noalloc(int dtype, int op, double p, int skip_mode,
                                 void* out, uint64_t out_base, uint64_t row_begin, uint64_t row_end,
                                 void* stream);
 
+/* The processing order sbg_pairwise_device uses when it picks one itself:
+ * perm[i] is the index of the PCF visited i-th, by breakpoint count within
+ * each window of 1024 consecutive PCFs (ties by index).  Device pointers,
+ * caller's stream.  Pass it as row_perm / col_perm to keep that order on a
+ * band of rows.  No counterpart in the reference. */
+int sbg_length_order_device(const uint64_t* offsets, uint64_t n, uint32_t* perm, void* stream);
+
 /* Kernels this library has launched in this process so far (all threads and
  * devices; a CUDA graph replay counts the kernels it holds).  Read it before
  * and after a region to count the region's launches.  No counterpart in the

@@ -76,7 +76,11 @@ namespace sbg
     }
   }
 
-  template <typename T, int OP>
+  // SQUARE: every ordered pair (i, j), i != j, and only the warp's own row
+  // side takes gradients (each PCF collects its gradients as the row of its
+  // pairs); no global atomics inside the merge.  Otherwise: the lower
+  // triangle, both sides, the column side with global atomics.
+  template <typename T, int OP, bool SQUARE>
   __global__ void __launch_bounds__(512) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
   {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -100,12 +104,13 @@ namespace sbg
       if (item >= B.total_items) break;
       const uint64_t G = ceil_div_u64(B.n, 32);
       uint64_t c, g;
-      tri_decode(item, 0, B.n, B.q, G, &c, &g);
+      if (SQUARE) { c = item / G; g = item % G; }
+      else tri_decode(item, 0, B.n, B.q, G, &c, &g);
       uint64_t row_lo = c * 32ull * B.q;
       uint64_t row_hi = row_lo + 32ull * B.q;
       if (row_hi > B.n) row_hi = B.n;
       const uint64_t col0 = 32ull * g;
-      if (row_lo < col0 + 1) row_lo = col0 + 1;  // the diagonal is not handled here
+      if (!SQUARE && row_lo < col0 + 1) row_lo = col0 + 1;  // the diagonal is not handled here
 
       const uint64_t cj = col0 + lane;
       const bool cvalid = cj < B.n;
@@ -127,7 +132,7 @@ namespace sbg
           const uint64_t roff = B.off[i];
           const uint32_t rlen = (uint32_t)(B.off[i + 1] - roff);
           if (rlen == 0 || rlen > B.row_cap || roff + rlen > B.npts) continue;
-          const bool ok = cvalid && cj < i;
+          const bool ok = cvalid && (SQUARE ? cj != i : cj < i);
           T w = T(0);
           if (ok)
           {
@@ -174,17 +179,18 @@ namespace sbg
             else
             {
               // Gc.tn < F.tn <= TMAX, so the column has a next element
-              if (w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
+              if (!SQUARE && w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
               accG = T(0);
               const Elem<T> Gn = col[gi + 1];
-              if (w != T(0) && !(Gc.tn == t)) atomicAdd(&B.grad[2 * (coff + gi + 1)], w * step_delta<OP>(Gc.v, Gn.v, F.v));
+              if (!SQUARE && w != T(0) && !(Gc.tn == t))
+                atomicAdd(&B.grad[2 * (coff + gi + 1)], w * step_delta<OP>(Gc.v, Gn.v, F.v));
               ++gi;
               Gc = Gn;
             }
             t = tn;
           }
           if (w != T(0)) atomicAdd(&sg[2 * fi + 1], w * accF);
-          if (w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
+          if (!SQUARE && w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
           __syncwarp();
           for (uint32_t k = lane; k < rlen; k += 32)
           {
@@ -263,17 +269,24 @@ namespace sbg
     const int warps = 16;
     const size_t smem = (size_t)warps * lmax * 2 * sizeof(T);
     if (smem + 2048 > dev.smem_optin) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
+#ifdef SBG_BWD_TRIANGLE
+    constexpr bool SQ = false;
+#else
+    constexpr bool SQ = true;
+#endif
+    const uint64_t G = ceil_div_u64(n, 32);
+    auto items = [&](uint32_t qq) { return SQ ? ceil_div_u64(n, 32ull * qq) * G : tri_item_count(0, n, qq, G); };
     uint32_t q = 1;
     for (uint32_t cand = 8; cand >= 1; cand /= 2)
-      if (tri_item_count(0, n, cand, ceil_div_u64(n, 32)) >= (uint64_t)dev.sms * 6) { q = cand; break; }
+      if (items(cand) >= (uint64_t)dev.sms * 6) { q = cand; break; }
     B.q = q;
-    B.total_items = tri_item_count(0, n, q, ceil_div_u64(n, 32));
+    B.total_items = items(q);
     SBG_CUDA(cudaMemsetAsync(queue, 0, 8, st));
     if (B.total_items > 0)
     {
-      void (*fn)(const BwdParams<T>) = bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER>
-                                     : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST>
-                                                         : pairs_backward_kernel<T, BWD_L1DIST>;
+      void (*fn)(const BwdParams<T>) = bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SQ>
+                                     : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SQ>
+                                                         : pairs_backward_kernel<T, BWD_L1DIST, SQ>;
       SBG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms);
       fn<<<grid, warps * 32, smem, st>>>(B);

@@ -287,7 +287,9 @@ namespace sbg
       const uint64_t cj = col0 + lane;
       const bool cvalid = cj < nc;
       const uint64_t cj_eff = cvalid ? cj : col0;
-      const uint64_t corig = Pp->cperm ? Pp->cperm[cj_eff] : cj_eff;
+      uint64_t corig = Pp->cperm ? Pp->cperm[cj_eff] : cj_eff;
+      const bool pgood = corig < nc;  // a permutation entry out of range reads column 0, result dropped
+      if (!pgood) corig = 0;
       const uint64_t coff = Pp->coff[corig];
       const uint32_t clen = (uint32_t)(Pp->coff[corig + 1] - coff);
       const uint32_t maxlc = warp_max_u32(clen);
@@ -326,9 +328,10 @@ namespace sbg
           if (i >= row_hi) break;
 
           const uint64_t iorig = Pp->rperm ? Pp->rperm[i] : i;
+          if (iorig >= Pp->nr) continue;  // a permutation entry out of range: skip the row
           const uint64_t roff = Pp->roff[iorig];
           const uint32_t rlen = (uint32_t)(Pp->roff[iorig + 1] - roff);
-          const bool ok = cvalid && (mode == MODE_CROSS || (mode == MODE_PDIST ? cj < i : cj <= i));
+          const bool ok = cvalid && pgood && (mode == MODE_CROSS || (mode == MODE_PDIST ? cj < i : cj <= i));
           if (!__any_sync(FULL, ok) || rlen == 0) continue;
           if (!SMEM && roff + rlen > Pp->rcap) continue;  // offsets past the packed rows
           const uint32_t steps = rlen + maxlc - 1;
@@ -517,7 +520,9 @@ namespace sbg
       const uint64_t cj = col0 + lane;
       const bool cvalid = cj < nc;
       const uint64_t cj_eff = cvalid ? cj : col0;
-      const uint64_t corig = Pp->cperm ? Pp->cperm[cj_eff] : cj_eff;
+      uint64_t corig = Pp->cperm ? Pp->cperm[cj_eff] : cj_eff;
+      const bool pgood = corig < nc;  // a permutation entry out of range reads column 0, result dropped
+      if (!pgood) corig = 0;
       const uint64_t coff = Pp->coff[corig];
       const uint32_t clen = (uint32_t)(Pp->coff[corig + 1] - coff);
       const uint32_t maxlc = warp_max_u32(clen);
@@ -544,9 +549,10 @@ namespace sbg
           const uint64_t i = row_lo + r;
           if (i >= row_hi) break;
           const uint64_t iorig = Pp->rperm ? Pp->rperm[i] : i;
+          if (iorig >= Pp->nr) continue;  // a permutation entry out of range: skip the row
           const uint64_t roff = Pp->roff[iorig];
           const uint32_t rlen = (uint32_t)(Pp->roff[iorig + 1] - roff);
-          const bool ok = cvalid && (mode == MODE_CROSS || (mode == MODE_PDIST ? cj < i : cj <= i));
+          const bool ok = cvalid && pgood && (mode == MODE_CROSS || (mode == MODE_PDIST ? cj < i : cj <= i));
           if (!__any_sync(FULL, ok) || rlen == 0 || roff + rlen > Pp->rcap) continue;
           const uint32_t steps = rlen + maxlc - 1;
           T res;

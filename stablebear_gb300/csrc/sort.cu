@@ -13,6 +13,7 @@
 // unique, so a bitonic network (not stable by itself) gives the one
 // deterministic order.  Each window is sorted by one CTA in shared memory;
 // the last window is padded with all-ones keys, which sort last.
+#include "../../include/sbgpu.h"
 #include "sbg_internal.hpp"
 
 #include <algorithm>
@@ -35,8 +36,9 @@ namespace sbg
     }
 
     // Stages k = k_first .. k_last (powers of two) with partner distances
-    // j = min(k / 2, j_first) .. 1, on one tile in shared memory.  The
-    // direction of a comparison comes from the global index.
+    // j = min(k / 2, j_first) .. 1, on one tile in shared memory.  Every tile
+    // is sorted on its own, ascending: the direction of a comparison comes
+    // from the index inside the tile.
     __global__ void __launch_bounds__(SORT_THREADS) tile_stages_kernel(uint64_t* keys, uint64_t n, uint64_t tile,
                                                                        uint64_t k_first, uint64_t k_last,
                                                                        uint64_t j_first)
@@ -52,8 +54,7 @@ namespace sbg
           for (uint64_t t = threadIdx.x; t < tile / 2; t += blockDim.x)
           {
             const uint64_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));  // j is a power of two
-            const uint64_t g = base + i;
-            cmp_swap(s[i], s[i + j], (g & k) == 0);
+            cmp_swap(s[i], s[i + j], (i & k) == 0);
           }
           __syncthreads();
         }
@@ -117,5 +118,34 @@ namespace sbg
     }
     keys_to_perm_kernel<<<blocks, 256, 0, st>>>(keys, n, perm);
     SBG_CUDA(launched());
+  }
+}
+
+extern "C" int sbg_length_order_device(const uint64_t* offsets, uint64_t n, uint32_t* perm, void* stream)
+{
+  using namespace sbg;
+  try
+  {
+    if (n && (!offsets || !perm)) throw Error(ST_INVALID_ARGUMENT, "null pointer");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    void* keys = nullptr;
+    if (n)
+    {
+      SBG_CUDA(cudaMallocAsync(&keys, length_order_scratch_bytes(n), st));
+      struct Free { void* p; cudaStream_t s; ~Free() { cudaFreeAsync(p, s); } } guard{keys, st};
+      length_order_device(offsets, n, perm, keys, st);
+    }
+    set_last_error("");
+    return ST_OK;
+  }
+  catch (const Error& e)
+  {
+    set_last_error(e.what());
+    return e.status;
+  }
+  catch (const std::exception& e)
+  {
+    set_last_error(e.what());
+    return ST_INTERNAL;
   }
 }

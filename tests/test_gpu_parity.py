@@ -330,6 +330,25 @@ def _window_order(lens, w=1024):
     return np.concatenate([k + np.argsort(lens[k:k + w], kind="stable") for k in range(0, len(lens), w)])
 
 
+def test_length_order_permutation():
+    """sbg_length_order_device is the windowed stable sort by length, for
+    sizes below one window, at whole windows, and with a padded last window
+    of either parity."""
+    import torch
+    from stablebear_gb300 import _native as nat
+    rng = np.random.default_rng(0)
+    for n in (1, 2, 37, 1024, 1025, 2049, 3000, 20000, 100000):
+        lens = rng.integers(1, 400, n)
+        off = np.zeros(n + 1, np.int64)
+        np.cumsum(lens, out=off[1:])
+        do = torch.from_numpy(off).cuda()
+        perm = torch.empty(n, dtype=torch.int32, device="cuda")
+        nat.check(nat.lib().sbg_length_order_device(do.data_ptr(), n, perm.data_ptr(),
+                                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        got = perm.cpu().numpy().view(np.uint32)
+        np.testing.assert_array_equal(got, _window_order(lens))
+
+
 def test_device_length_order_is_the_stable_length_sort():
     """The device entry's own processing order (computed on the GPU) gives
     the same bits as passing the windowed stable length sort as the
@@ -337,7 +356,7 @@ def test_device_length_order_is_the_stable_length_sort():
     import torch
     from stablebear_gb300 import _native as nat, synthetic
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for n, lo, hi in ((3000, 1, 300), (37, 1, 9), (2049, 5, 6)):
+    for n, lo, hi in ((3000, 1, 300), (37, 1, 9), (2049, 5, 6), (20000, 1, 40)):
         pts, off = synthetic.gaussian(n, synthetic.uniform_lengths(lo, hi), np.float32, seed=n)
         lens = np.diff(off.astype(np.int64))
         perm = torch.from_numpy(_window_order(lens).astype(np.uint32).view(np.int32)).cuda()
