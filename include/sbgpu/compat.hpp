@@ -344,6 +344,18 @@ namespace sb
     throw std::runtime_error(msg);
   }
 
+  // The reference's task executor (include/sbear/executor.hpp): callers pass
+  // default_executor() to start_async.  Tasks here run on their own worker
+  // thread, so the executor carries nothing.
+  struct Executor
+  {
+  };
+  inline Executor& default_executor()
+  {
+    static Executor e;
+    return e;
+  }
+
   template <typename RetT = void>
   class StoppableTask;
 

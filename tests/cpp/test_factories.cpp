@@ -26,7 +26,7 @@ static void run(const char* tag)
   auto pcfs = five<T>();
   sb::DistanceMatrix<T> dm(pcfs.size());
   auto t1 = sb::create_cuda_block_integrate_l1_task(dm, pcfs);
-  t1->start_async(0);
+  t1->start_async(sb::default_executor());
   while (!t1->wait_for(std::chrono::milliseconds(10))) { }
   for (size_t k = 0; k < dm.storage_count(); ++k) std::printf("%s l1 %.17g\n", tag, (double)dm.data()[k]);
 
