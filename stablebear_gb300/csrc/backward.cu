@@ -269,10 +269,14 @@ namespace sbg
     const int warps = 16;
     const size_t smem = (size_t)warps * lmax * 2 * sizeof(T);
     if (smem + 2048 > dev.smem_optin) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
-#ifdef SBG_BWD_TRIANGLE
-    constexpr bool SQ = false;
-#else
+    // The ordered-pairs variant measured slower on GB300 (N = 4096, L2 kernel:
+    // forward + backward 74 ms against 46 ms): twice the merges, and the
+    // lanes' shared-memory adds into one row buffer contend.  It stays
+    // available for measurement behind SBG_BWD_SQUARE.
+#ifdef SBG_BWD_SQUARE
     constexpr bool SQ = true;
+#else
+    constexpr bool SQ = false;
 #endif
     const uint64_t G = ceil_div_u64(n, 32);
     auto items = [&](uint32_t qq) { return SQ ? ceil_div_u64(n, 32ull * qq) * G : tri_item_count(0, n, qq, G); };

@@ -93,11 +93,29 @@ namespace sbg
           if (u < nt) ts.decode(k0 + u, &a[u], &b[u]);
           else { a[u] = 0; b[u] = 0; }
           const uint64_t i0 = a[u] * TILE, j = b[u] * TILE + tx;
-#pragma unroll
-          for (int q = 0; q < TILE / ROWS; ++q)
+          if (u < nt && a[u] > b[u] && i0 + TILE <= n)
           {
-            const uint64_t i = i0 + ty + q * ROWS;
-            v[u][q] = (u < nt && i < n && j < n && (j < i || (diag && j == i))) ? cond[cond_index(diag, i, j)] : T(0);
+            // interior tile: every element exists, no per-element checks;
+            // consecutive rows' starts differ by i (+1 with the diagonal)
+            uint64_t i = i0 + ty;
+            const T* src = cond + cond_index(diag, i, 0) + j;
+#pragma unroll
+            for (int q = 0; q < TILE / ROWS; ++q)
+            {
+              v[u][q] = src[0];
+              // start of row i + ROWS minus start of row i
+              src += ROWS * i + (diag ? ROWS * (ROWS + 1) / 2 : ROWS * (ROWS - 1) / 2);
+              i += ROWS;
+            }
+          }
+          else
+          {
+#pragma unroll
+            for (int q = 0; q < TILE / ROWS; ++q)
+            {
+              const uint64_t i = i0 + ty + q * ROWS;
+              v[u][q] = (u < nt && i < n && j < n && (j < i || (diag && j == i))) ? cond[cond_index(diag, i, j)] : T(0);
+            }
           }
         }
 #pragma unroll
@@ -108,6 +126,23 @@ namespace sbg
         for (int u = 0; u < nt; ++u)
         {
           const uint64_t i0 = a[u] * TILE, j0 = b[u] * TILE;
+          if (a[u] > b[u] && i0 + TILE <= n && j0 >= row_begin && i0 + TILE <= row_end)
+          {
+            // interior tile with both copies inside the band (the band is
+            // contiguous and j0 < i0): plain row-pointer walks
+            T* d1 = dense + (i0 + ty - row_begin) * ld + j0 + tx;
+            T* d2 = dense + (j0 + ty - row_begin) * ld + i0 + tx;
+#pragma unroll
+            for (int q = 0; q < TILE / ROWS; ++q)
+            {
+              const int r = ty + q * ROWS;
+              d1[0] = tile[u][r][tx];
+              d2[0] = tile[u][tx][r];
+              d1 += ROWS * ld;
+              d2 += ROWS * ld;
+            }
+            continue;
+          }
           // dense tile (a, b): rows of block a inside the band; on the
           // diagonal tile the upper half is the transposed lower half
           for (int r = ty; r < TILE; r += ROWS)
