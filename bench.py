@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--cpu-sample-rows", type=int, default=0, help="rows in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--order", type=int, default=0, choices=[0, 1],
+                    help="processing order of the device entry: 0 length order (default), 1 caller order")
     ap.add_argument("--config", default="large",
                     choices=["large", "plain", "stable_rank", "batched", "fwdbwd", "dense"],
                     help="large: the headline workload; the others print their own report line")
@@ -405,6 +407,9 @@ def main():
     sptr = ctypes.c_void_p(stream.cuda_stream)
     lib = nat.lib()
 
+    if args.order:
+        sb.set_tuning(order=args.order)
+
     def step():
         nat.check(lib.sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
                                           do.data_ptr(), n, None, None, 0, None, None, lmax, out.data_ptr(), 0, 0, 0,
@@ -509,6 +514,17 @@ def main():
     peak = roofline.fp32_peak(local)
     achieved = segs * W_SEG / (ms_step / 1e3) / 1e12
     traffic = roofline.traffic_per_launch("pairs_kernel_l1_f32", n)
+    # The pipe that actually bounds the kernel: every merged rectangle brings
+    # one new 8-byte (t, v) element per lane out of shared memory; the peak is
+    # 128 B per clock per SM at the sampled SM clock.
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 0
+    smem_peak = 128.0 * sms * mhz * 1e6 / 1e12 if mhz else None
+    smem_ach = segs * 8.0 / (ms_step / 1e3) / 1e12
+    smem_view = {"achieved": smem_ach, "peak": smem_peak, "unit": "TB/s",
+                 "frac": (smem_ach / smem_peak) if smem_peak else None,
+                 "work_model": "8 B of (t, v) per lane per merged rectangle, from shared memory",
+                 "peak_source": f"128 B/clk/SM x {sms} SMs x sampled SM clock"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -518,6 +534,7 @@ def main():
                      "frac": achieved / peak["value"], "traffic": traffic, "peak_source": peak["source"],
                      "work_model": f"{W_SEG} FP32 lane-ops per merged segment x {segs} segments per launch"},
         "hbm_output_stream": {"bytes_per_launch": pairs * 4, "achieved_gbs": pairs * 4 / (ms_step / 1e3) / 1e9},
+        "smem_view": smem_view,
         "clocks": clk, "gpu_launches": launches, "step_ms": per,
     }
     if cpu:
