@@ -80,7 +80,12 @@ namespace sbg
   // side takes gradients (each PCF collects its gradients as the row of its
   // pairs); no global atomics inside the merge.  Otherwise: the lower
   // triangle, both sides, the column side with global atomics.
-  template <typename T, int OP, bool SQUARE>
+  //
+  // WARP_ITEMS: every warp takes its own items from the queue and walks the
+  // item's rows itself, so the warps of a CTA work on different column
+  // groups and their column atomics do not meet on the same addresses.
+  // Otherwise the CTA takes an item and its warps share the rows.
+  template <typename T, int OP, bool SQUARE, bool WARP_ITEMS>
   __global__ void __launch_bounds__(512) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
   {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -94,13 +99,22 @@ namespace sbg
 
     for (;;)
     {
-      if (threadIdx.x == 0)
+      unsigned long long item;
+      if (WARP_ITEMS)
       {
-        s_item = atomicAdd(B.queue, 1ull);
-        s_next_row = 0;
+        if (lane == 0) item = atomicAdd(B.queue, 1ull);
+        item = __shfl_sync(FULL, item, 0);
       }
-      __syncthreads();
-      const unsigned long long item = s_item;
+      else
+      {
+        if (threadIdx.x == 0)
+        {
+          s_item = atomicAdd(B.queue, 1ull);
+          s_next_row = 0;
+        }
+        __syncthreads();
+        item = s_item;
+      }
       if (item >= B.total_items) break;
       const uint64_t G = ceil_div_u64(B.n, 32);
       uint64_t c, g;
@@ -122,11 +136,14 @@ namespace sbg
 
       if (item_ok)
       {
-        for (;;)
+        for (unsigned next = 0;; ++next)
         {
-          unsigned r = 0;
-          if (lane == 0) r = atomicAdd(&s_next_row, 1u);
-          r = __shfl_sync(FULL, r, 0);
+          unsigned r = next;
+          if (!WARP_ITEMS)
+          {
+            if (lane == 0) r = atomicAdd(&s_next_row, 1u);
+            r = __shfl_sync(FULL, r, 0);
+          }
           const uint64_t i = row_lo + r;
           if (i >= row_hi) break;
           const uint64_t roff = B.off[i];
@@ -201,7 +218,7 @@ namespace sbg
           __syncwarp();
         }
       }
-      __syncthreads();
+      if (!WARP_ITEMS) __syncthreads();
     }
   }
 
@@ -278,19 +295,25 @@ namespace sbg
 #else
     constexpr bool SQ = false;
 #endif
+#ifdef SBG_BWD_CTA_ITEMS
+    constexpr bool WI = false;
+#else
+    constexpr bool WI = true;
+#endif
     const uint64_t G = ceil_div_u64(n, 32);
     auto items = [&](uint32_t qq) { return SQ ? ceil_div_u64(n, 32ull * qq) * G : tri_item_count(0, n, qq, G); };
+    const uint64_t want_items = (uint64_t)dev.sms * (WI ? warps * 4 : 6);
     uint32_t q = 1;
     for (uint32_t cand = 8; cand >= 1; cand /= 2)
-      if (items(cand) >= (uint64_t)dev.sms * 6) { q = cand; break; }
+      if (items(cand) >= want_items) { q = cand; break; }
     B.q = q;
     B.total_items = items(q);
     SBG_CUDA(cudaMemsetAsync(queue, 0, 8, st));
     if (B.total_items > 0)
     {
-      void (*fn)(const BwdParams<T>) = bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SQ>
-                                     : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SQ>
-                                                         : pairs_backward_kernel<T, BWD_L1DIST, SQ>;
+      void (*fn)(const BwdParams<T>) = bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SQ, WI>
+                                     : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SQ, WI>
+                                                         : pairs_backward_kernel<T, BWD_L1DIST, SQ, WI>;
       SBG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms);
       fn<<<grid, warps * 32, smem, st>>>(B);
