@@ -604,9 +604,9 @@ namespace sbg
     drows.upload(rows, compute.s);
     if (mode == MODE_CROSS) dcols.upload(cs, compute.s);
 
-    // Processing order: length-sorted (unless the order setting asks for the
-    // caller's) when the whole output stays in one device buffer.  The
-    // permutation is the one the device entry computes on the GPU.
+    // Processing order: by length within windows (unless the order setting
+    // asks for the caller's), the permutation the device entry computes on
+    // the GPU, so both entries give the same bits.
     size_t freeb = 0, totalb = 0;
     SBG_CUDA(cudaMemGetInfo(&freeb, &totalb));
     const size_t out_bytes = (size_t)total * sizeof(T);
@@ -614,7 +614,7 @@ namespace sbg
     int order = settings().order.load();
     std::vector<uint32_t> rperm, cperm;
     bool sorted = false;
-    if (order != 1 && out_bytes <= budget && rows.n <= 0xffffffffull && cs.n <= 0xffffffffull)
+    if (order != 1 && rows.n <= 0xffffffffull && cs.n <= 0xffffffffull)
     {
       sorted = true;
       cperm = length_order(cs.off, cs.n);
@@ -651,14 +651,24 @@ namespace sbg
       direct = true;
     }
 
-    // Bands of whole row chunks.  One band when sorted (the permuted result
-    // is scattered over the whole matrix), when writing directly, or when
-    // the output is small.
+    // Bands of whole row chunks.  One band when writing directly or when the
+    // output is small.  In length order the bands are also whole order
+    // windows: the order only permutes PCFs inside a window, so the rows of
+    // a band of windows are the same set in either order, and every pair
+    // with its later PCF in the band lands in the band's contiguous range
+    // of the condensed (or dense) output.
     uint64_t band_bytes = settings().bandBytes.load();
     if (band_bytes == 0) band_bytes = out_bytes > (512ull << 20) ? out_bytes / 8 + 1 : out_bytes;
     band_bytes = std::min<uint64_t>(band_bytes, budget / 2 > 0 ? budget / 2 : band_bytes);
     std::vector<std::pair<uint64_t, uint64_t>> bands;
-    if (direct || sorted || band_bytes >= out_bytes)
+    uint64_t align = chunk_rows;
+    if (sorted)
+    {
+      uint64_t g = align, h = LENGTH_ORDER_WINDOW;
+      while (h) { const uint64_t r = g % h; g = h; h = r; }
+      align = align / g * LENGTH_ORDER_WINDOW;  // lcm(chunk_rows, window)
+    }
+    if (direct || band_bytes >= out_bytes)
     {
       if (!direct && out_bytes > budget) throw Error(ST_OUT_OF_MEMORY, "output does not fit in device memory");
       bands.emplace_back(0, rows.n);
@@ -668,10 +678,10 @@ namespace sbg
       uint64_t rb = 0;
       while (rb < rows.n)
       {
-        uint64_t re = std::min<uint64_t>(rows.n, rb + chunk_rows);
+        uint64_t re = std::min<uint64_t>(rows.n, rb + align);
         while (re < rows.n)
         {
-          uint64_t nxt = std::min<uint64_t>(rows.n, re + chunk_rows);
+          uint64_t nxt = std::min<uint64_t>(rows.n, re + align);
           uint64_t bytes = (row_output_start(mode, nxt, cs.n) - row_output_start(mode, rb, cs.n)) * sizeof(T);
           if (bytes > band_bytes) break;
           re = nxt;
@@ -718,8 +728,8 @@ namespace sbg
       d.rperm = sorted ? drperm.as<uint32_t>() : nullptr;
       d.cperm = sorted ? (mode == MODE_CROSS ? dcperm.as<uint32_t>() : drperm.as<uint32_t>()) : nullptr;
       d.out = direct ? out : obuf[b].as<T>();
-      d.out_base = (sorted || direct) ? 0 : row_output_start(mode, bands[k].first, cs.n);
-      d.out_count = (sorted || direct) ? total : row_output_start(mode, bands[k].second, cs.n) - d.out_base;
+      d.out_base = direct ? 0 : row_output_start(mode, bands[k].first, cs.n);
+      d.out_count = direct ? total : row_output_start(mode, bands[k].second, cs.n) - d.out_base;
       d.ld = cs.n;
       d.row_begin = bands[k].first; d.row_end = bands[k].second;
       d.q = pl.q; d.mode = mode; d.p = (T)p;
@@ -744,8 +754,8 @@ namespace sbg
       const int b = (int)(k % 2);
       if (k + 1 < bands.size() && !(ctl.stop && ctl.stop->load())) launch_band(k + 1);
       const uint64_t rb = bands[k].first, re = bands[k].second;
-      const uint64_t lo = sorted ? 0 : row_output_start(mode, rb, cs.n);
-      const uint64_t hi = sorted ? total : row_output_start(mode, re, cs.n);
+      const uint64_t lo = row_output_start(mode, rb, cs.n);
+      const uint64_t hi = row_output_start(mode, re, cs.n);
       SBG_CUDA(cudaStreamWaitEvent(copy.s, computed[b].e, 0));
       if (hi > lo) stager.copy(out + lo, obuf[b].as<T>(), (hi - lo) * sizeof(T), copy.s);
       stager.flush();

@@ -420,3 +420,22 @@ def test_kernel_launch_counter():
     finally:
         sb.set_tuning()
     assert call() > 1
+
+
+def test_bands_in_length_order_match_one_band():
+    """The host pipeline in length order, cut into bands of whole order
+    windows, gives the bits of one band, for pdist, the kernel matrix and
+    cdist."""
+    import stablebear_gb300 as sb
+    from stablebear_gb300 import synthetic
+    pts, off = synthetic.gaussian(2600, synthetic.uniform_lengths(1, 120), np.float32, seed=31)
+    X = arr(pts, off)
+    Y = arr(*synthetic.gaussian(700, synthetic.uniform_lengths(1, 90), np.float32, seed=32))
+    one = (sb.pdist(X).data.copy(), sb.l2_kernel(X).data.copy(), sb.cdist(X, Y).copy())
+    try:
+        sb.set_tuning(band_bytes=256 << 10)
+        many = (sb.pdist(X).data.copy(), sb.l2_kernel(X).data.copy(), sb.cdist(X, Y).copy())
+    finally:
+        sb.set_tuning()
+    for a, b in zip(one, many):
+        np.testing.assert_array_equal(a, b)
