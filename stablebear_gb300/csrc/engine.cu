@@ -392,14 +392,18 @@ namespace sbg
     if (row_begin % (32ull * pl.q) != 0)
       throw Error(ST_INVALID_ARGUMENT, "row_begin must be a multiple of the row chunk (32*q)");
 
-    // Processing order: by breakpoint count, computed on the stream, when
-    // the call covers the whole matrix (a band in caller order owns one
-    // contiguous output range; in another order it would not) and neither
-    // the caller nor the order setting fixed one.  The permutation is the
-    // one the host entry uses, so both give the same bits.
+    // Processing order: by breakpoint count within windows of
+    // LENGTH_ORDER_WINDOW PCFs, computed on the stream, unless the caller or
+    // the order setting fixed one.  The band must be whole windows: the
+    // order permutes PCFs only inside a window, so such a band holds the
+    // same rows in either order and its results stay in the band's
+    // contiguous output range.  The permutation is the one the host entry
+    // uses, so both give the same bits.
     std::unique_ptr<AsyncBuf<T>> order_buf;
-    const bool whole = row_begin == 0 && row_end == rows.n && out_base == 0;
-    if (!rperm && !cperm && whole && settings().order.load() != 1 && rows.n <= 0xffffffffull &&
+    const bool windows = row_begin % LENGTH_ORDER_WINDOW == 0 &&
+                         (row_end % LENGTH_ORDER_WINDOW == 0 || row_end == rows.n);
+    const bool caller_perm = rperm || cperm;
+    if (!caller_perm && windows && settings().order.load() != 1 && rows.n <= 0xffffffffull &&
         cs.n <= 0xffffffffull)
     {
       const uint64_t nr = rows.n, nc = (mode == MODE_CROSS) ? cs.n : 0;
@@ -424,9 +428,10 @@ namespace sbg
     d.row_begin = row_begin; d.row_end = row_end;
     d.q = pl.q; d.mode = mode; d.p = (T)p;
     {
-      // rows [row_begin, row_end) in caller order own one contiguous range;
-      // with a processing order the results may land anywhere in the matrix
-      const uint64_t hi = (rperm || cperm) ? output_count(mode, rows.n, cs.n) : row_output_start(mode, row_end, cs.n);
+      // rows [row_begin, row_end) in caller order, or in the windowed length
+      // order, own one contiguous range; with a caller's order the results
+      // may land anywhere in the matrix
+      const uint64_t hi = caller_perm ? output_count(mode, rows.n, cs.n) : row_output_start(mode, row_end, cs.n);
       d.out_count = hi > out_base ? hi - out_base : 0;
     }
 

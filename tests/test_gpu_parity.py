@@ -439,3 +439,31 @@ def test_bands_in_length_order_match_one_band():
         sb.set_tuning()
     for a, b in zip(one, many):
         np.testing.assert_array_equal(a, b)
+
+
+def test_device_bands_of_whole_windows_use_the_length_order():
+    """Device-entry bands of whole 1024-PCF windows run in the length order
+    and give the bits of the whole call, each band into its own buffer."""
+    import torch
+    from stablebear_gb300 import _native as nat, synthetic
+    pts, off = synthetic.gaussian(2600, synthetic.uniform_lengths(1, 100), np.float32, seed=33)
+    n = len(off) - 1
+    dp = torch.from_numpy(pts).cuda()
+    do = torch.from_numpy(off.astype(np.int64)).cuda()
+    lmax = int(np.diff(off.astype(np.int64)).max())
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    total = n * (n - 1) // 2
+    whole = torch.empty(total, device="cuda")
+    nat.check(nat.lib().sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                            do.data_ptr(), n, None, None, 0, None, None, lmax, whole.data_ptr(), 0, 0,
+                                            0, st))
+    parts = []
+    for rb, re in ((0, 1024), (1024, 2048), (2048, n)):
+        base = rb * (rb - 1) // 2
+        buf = torch.full((re * (re - 1) // 2 - base,), float("nan"), device="cuda")
+        nat.check(nat.lib().sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                                do.data_ptr(), n, None, None, 0, None, None, lmax, buf.data_ptr(),
+                                                base, rb, re, st))
+        parts.append(buf)
+    torch.cuda.synchronize()
+    assert torch.equal(torch.cat(parts), whole)
