@@ -85,6 +85,20 @@ namespace sbg
   // item's rows itself, so the warps of a CTA work on different column
   // groups and their column atomics do not meet on the same addresses.
   // Otherwise the CTA takes an item and its warps share the rows.
+  // Gradients are accumulated in a paired layout, slot k of a PCF holding
+  // (dL/dv_k, dL/dt_{k+1}): a column advance adds to both halves of one
+  // 8-byte slot, one vector reduction for float, and a row flush moves whole
+  // slots.  pair_to_point_layout writes the (dL/dt, dL/dv) layout at the end.
+  __device__ __forceinline__ void red_add2(float* p, float a, float b)
+  {
+    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(a), "f"(b) : "memory");
+  }
+  __device__ __forceinline__ void red_add2(double* p, double a, double b)
+  {
+    atomicAdd(p, a);
+    atomicAdd(p + 1, b);
+  }
+
   template <typename T, int OP, bool SQUARE, bool WARP_ITEMS>
   __global__ void __launch_bounds__(512) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
   {
@@ -94,7 +108,7 @@ namespace sbg
     __shared__ unsigned int s_next_row;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    T* sg = sgrad_all + (size_t)warp * B.row_cap * 2;  // [k][2]: t-grad, v-grad
+    T* sg = sgrad_all + (size_t)warp * B.row_cap * 2;  // slot k: dL/dv_k, dL/dt_{k+1}
     const unsigned FULL = 0xffffffffu;
 
     for (;;)
@@ -185,40 +199,62 @@ namespace sbg
             {
               if (fi + 1 < rlen)
               {
-                if (w != T(0)) atomicAdd(&sg[2 * fi + 1], w * accF);
+                if (w != T(0)) atomicAdd(&sg[2 * fi], w * accF);
                 accF = T(0);
                 const Elem<T> Fn = row[fi + 1];
-                if (w != T(0) && !(F.tn == Gc.tn)) atomicAdd(&sg[2 * (fi + 1)], w * step_delta<OP>(F.v, Fn.v, Gc.v));
+                if (w != T(0) && !(F.tn == Gc.tn)) atomicAdd(&sg[2 * fi + 1], w * step_delta<OP>(F.v, Fn.v, Gc.v));
                 ++fi;
                 F = Fn;
               }
             }
             else
             {
-              // Gc.tn < F.tn <= TMAX, so the column has a next element
-              if (!SQUARE && w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
-              accG = T(0);
+              // Gc.tn < F.tn <= TMAX, so the column has a next element:
+              // dL/dv of this element and dL/dt of the next share a slot
               const Elem<T> Gn = col[gi + 1];
-              if (!SQUARE && w != T(0) && !(Gc.tn == t))
-                atomicAdd(&B.grad[2 * (coff + gi + 1)], w * step_delta<OP>(Gc.v, Gn.v, F.v));
+              if (!SQUARE && w != T(0))
+                red_add2(&B.grad[2 * (coff + gi)], w * accG,
+                         (Gc.tn == t) ? T(0) : w * step_delta<OP>(Gc.v, Gn.v, F.v));
+              accG = T(0);
               ++gi;
               Gc = Gn;
             }
             t = tn;
           }
-          if (w != T(0)) atomicAdd(&sg[2 * fi + 1], w * accF);
-          if (!SQUARE && w != T(0)) atomicAdd(&B.grad[2 * (coff + gi) + 1], w * accG);
+          if (w != T(0)) atomicAdd(&sg[2 * fi], w * accF);
+          if (!SQUARE && w != T(0)) atomicAdd(&B.grad[2 * (coff + gi)], w * accG);
           __syncwarp();
           for (uint32_t k = lane; k < rlen; k += 32)
           {
-            const T gt = sg[2 * k], gv = sg[2 * k + 1];
-            if (gt != T(0)) atomicAdd(&B.grad[2 * (roff + k)], gt);
-            if (gv != T(0)) atomicAdd(&B.grad[2 * (roff + k) + 1], gv);
+            const T gv = sg[2 * k], gt = sg[2 * k + 1];
+            if (gv != T(0) || gt != T(0)) red_add2(&B.grad[2 * (roff + k)], gv, gt);
           }
           __syncwarp();
         }
       }
       if (!WARP_ITEMS) __syncthreads();
+    }
+  }
+
+  // (dL/dv_k, dL/dt_{k+1}) slots to the point layout (dL/dt_k, dL/dv_k).
+  // The slot of a PCF's last element holds no time gradient (there is no
+  // breakpoint after it).  One warp per PCF.
+  template <typename T>
+  __global__ void pair_to_point_layout(const T* __restrict__ gp, const uint64_t* __restrict__ off, uint64_t n,
+                                       uint64_t npts, T* __restrict__ grad)
+  {
+    const uint64_t wid = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+    for (uint64_t i = wid; i < n; i += nw)
+    {
+      const uint64_t o = off[i], len = off[i + 1] - o;
+      if (o + len > npts) continue;
+      for (uint64_t k = lane; k < len; k += 32)
+      {
+        grad[2 * (o + k)] = k == 0 ? T(0) : gp[2 * (o + k - 1) + 1];
+        grad[2 * (o + k) + 1] = gp[2 * (o + k)];
+      }
     }
   }
 
@@ -268,19 +304,22 @@ namespace sbg
 
     void* packed = nullptr;
     void* queue = nullptr;
+    void* paired = nullptr;
     SBG_CUDA(cudaMallocAsync(&packed, std::max<uint64_t>(1, npts) * sizeof(Elem<T>), st));
     SBG_CUDA(cudaMallocAsync(&queue, 256, st));
+    SBG_CUDA(cudaMallocAsync(&paired, std::max<uint64_t>(1, npts) * 2 * sizeof(T), st));
     struct Free
     {
-      void* a; void* b; cudaStream_t s;
-      ~Free() { cudaFreeAsync(a, s); cudaFreeAsync(b, s); }
-    } guard{packed, queue, st};
+      void* a; void* b; void* c; cudaStream_t s;
+      ~Free() { cudaFreeAsync(a, s); cudaFreeAsync(b, s); cudaFreeAsync(c, s); }
+    } guard{packed, queue, paired, st};
+    SBG_CUDA(cudaMemsetAsync(paired, 0, std::max<uint64_t>(1, npts) * 2 * sizeof(T), st));
     SBG_CUDA(launch_pack<T>(pts, off, n, static_cast<Elem<T>*>(packed), npts, dev.sms, st));
 
     BwdParams<T> B{};
     B.pk = static_cast<const Elem<T>*>(packed);
     B.off = off; B.n = n; B.npts = npts; B.mode = mode;
-    B.grad_out = grad_out; B.fwd = fwd; B.grad = grad;
+    B.grad_out = grad_out; B.fwd = fwd; B.grad = static_cast<T*>(paired);
     B.queue = static_cast<unsigned long long*>(queue);
     B.row_cap = lmax;
     const int warps = 16;
@@ -295,10 +334,12 @@ namespace sbg
 #else
     constexpr bool SQ = false;
 #endif
-#ifdef SBG_BWD_CTA_ITEMS
-    constexpr bool WI = false;
-#else
+    // Per-warp items measured slower (58 against 50 ms): the column atomics
+    // were not colliding; they stay available behind SBG_BWD_WARP_ITEMS.
+#ifdef SBG_BWD_WARP_ITEMS
     constexpr bool WI = true;
+#else
+    constexpr bool WI = false;
 #endif
     const uint64_t G = ceil_div_u64(n, 32);
     auto items = [&](uint32_t qq) { return SQ ? ceil_div_u64(n, 32ull * qq) * G : tri_item_count(0, n, qq, G); };
@@ -319,9 +360,14 @@ namespace sbg
       fn<<<grid, warps * 32, smem, st>>>(B);
       SBG_CUDA(launched());
     }
+    {
+      const unsigned blocks = (unsigned)std::min<uint64_t>((n + 7) / 8, (uint64_t)dev.sms * 8);
+      pair_to_point_layout<T><<<blocks, 256, 0, st>>>(static_cast<const T*>(paired), off, n, npts, grad);
+      SBG_CUDA(launched());
+    }
     if (bop == BWD_INNER)
     {
-      // after the pair kernel on the same stream: plain adds are race-free
+      // after the layout pass on the same stream: plain adds are race-free
       const unsigned blocks = (unsigned)std::min<uint64_t>((n + 7) / 8, (uint64_t)dev.sms * 8);
       diag_backward_kernel<T><<<blocks, 256, 0, st>>>(B.pk, off, n, npts, grad_out, grad);
       SBG_CUDA(launched());
