@@ -71,7 +71,7 @@ typedef enum sbg_skip_mode {
 int sbg_api_version(void);
 /* Message of the last failing call on this thread ("" if none). */
 const char* sbg_last_error(void);
-/* "CUDA" — this build has no CPU path (pymodule.cpp: _build_type). */
+/* "CUDA" — the library has no CPU path (pymodule.cpp: _build_type). */
 const char* sbg_build_type(void);
 /* Number of visible CUDA devices (pymodule.cpp: get_ngpus). */
 int sbg_get_ngpus(int* n);
@@ -79,7 +79,7 @@ int sbg_get_ngpus(int* n);
 /* ---- settings: sb::Settings (include/sbear/settings.hpp:8-23) and the
  *      setters bound in src/python/pymodule.cpp:136-151 ------------------------ */
 
-int sbg_set_force_cpu(int on);            /* accepted; this build always runs on the GPU */
+int sbg_set_force_cpu(int on);            /* accepted; the library always runs on the GPU */
 int sbg_get_force_cpu(void);
 int sbg_set_cuda_threshold(uint64_t n);   /* accepted; no CPU path to fall back to */
 uint64_t sbg_get_cuda_threshold(void);

@@ -1,4 +1,4 @@
-"""Oracle package — test infrastructure only (checker and CPU baseline).
+"""Oracle package — test infrastructure only (parity reference and CPU baseline).
 
 Nothing under ``stablebear_gb300/`` imports this package.
 """

@@ -1,7 +1,7 @@
 """ORACLE — test infrastructure only (ctypes front-end of ``pcf_oracle.c``).
 
 Used by ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s
-CPU-baseline leg as the checker.  The product package never imports it.
+CPU-baseline leg, as the parity reference.  The product package never imports it.
 
 Inputs use the reference's CSR layout: ``points`` is an ``(M, 2)`` array of
 ``(t, v)`` rows (float32 or float64), ``offsets`` a ``uint64`` array of length

@@ -2,8 +2,8 @@
  * ORACLE — test infrastructure only.
  *
  * A plain-C restatement of stablebear's CPU pairwise-integration path, used by
- * the tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as
- * the checker / CPU baseline.  Nothing in the product (stablebear_gb300/)
+ * the tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg, as
+ * the parity reference and the CPU baseline.  Nothing in the product (stablebear_gb300/)
  * links, imports or calls this file.
  *
  * What it restates (paths relative to the stablebear source tree):

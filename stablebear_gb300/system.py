@@ -1,7 +1,7 @@
 """Process-wide settings (``stablebear/system.py:4-122`` over
 ``src/python/pymodule.cpp:136-159``).
 
-This build has exactly one execution path, the GPU.  ``force_cpu`` and
+This library has exactly one execution path, the GPU.  ``force_cpu`` and
 ``set_cuda_threshold`` are kept so existing code runs unchanged; their values
 are stored and reported back but select nothing.
 """
