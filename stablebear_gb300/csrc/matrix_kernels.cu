@@ -180,6 +180,37 @@ namespace sbg
         uint64_t a, b;
         ts.decode(k, &a, &b);
         const uint64_t i0 = a * TILE, j0 = b * TILE;
+        if (a > b && i0 + TILE <= n)
+        {
+          // interior tile: no bound checks, row-pointer walks, and the
+          // condensed row starts advance by i (+1 with the diagonal)
+          const T* up = dense + (j0 + ty) * ld + i0 + tx;
+          const T* lo = dense + (i0 + ty) * ld + j0 + tx;
+          T low[TILE / ROWS];
+#pragma unroll
+          for (int q = 0; q < TILE / ROWS; ++q)
+          {
+            upper[tx][ty + q * ROWS] = up[0];
+            low[q] = lo[0];
+            up += ROWS * ld;
+            lo += ROWS * ld;
+          }
+          __syncthreads();
+          uint64_t i = i0 + ty;
+          T* dst = cond + cond_index(diag, i, 0) + j0 + tx;
+#pragma unroll
+          for (int q = 0; q < TILE / ROWS; ++q)
+          {
+            const T v = low[q];
+            if (!(v == upper[ty + q * ROWS][tx])) f |= 1u;
+            if (!diag && v < T(0)) f |= 4u;
+            dst[0] = v;
+            dst += ROWS * i + (diag ? ROWS * (ROWS + 1) / 2 : ROWS * (ROWS - 1) / 2);
+            i += ROWS;
+          }
+          __syncthreads();
+          continue;
+        }
         // The mirror tile (b, a), read coalesced and kept transposed, and
         // this thread's values of the lower tile, all loads before the barrier.
         T low[TILE / ROWS];
