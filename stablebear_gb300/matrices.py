@@ -134,7 +134,9 @@ class _Condensed:
         return type(other) is type(self) and self._n == other._n and np.array_equal(self._data, other._data)
 
     def __repr__(self):
-        return f"{type(self).__name__}(n={self._n}, dtype={self._data.dtype})"
+        # as the reference's bound classes print (py_distance_matrix.hpp:78-83)
+        suffix = "_f32" if self._data.dtype == np.float32 else "_f64"
+        return f"{type(self).__name__}{suffix}(size={self._n})"
 
     # --- serialisation: stablebear's binary format (see ``io.py``) ----------
 

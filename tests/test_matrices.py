@@ -96,3 +96,8 @@ def test_from_dense_messages():
     a[1, 2] = a[2, 1] = -1.0
     with pytest.raises(ValueError, match="Matrix must be symmetric"):
         sb.DistanceMatrix.from_dense(a)
+
+
+def test_repr_as_the_reference():
+    assert repr(sb.DistanceMatrix(3, dtype=np.float32)) == "DistanceMatrix_f32(size=3)"
+    assert repr(sb.SymmetricMatrix(4)) == "SymmetricMatrix_f64(size=4)"
