@@ -255,11 +255,21 @@ def workload(n, seed):
     return pts, off
 
 
+def _generator_hash():
+    """Hash of the synthetic-data generator, so a result names the exact inputs."""
+    import hashlib
+    from stablebear_gb300 import synthetic
+    with open(synthetic.__file__, "rb") as fh:
+        return hashlib.sha256(fh.read()).hexdigest()[:16]
+
+
 def config(args, n, ws):
     return {"workload": f"L1 pdist, N={n} float32 PCFs, L~Poisson(256)+2, N(0,1) values, Exp(1) gaps, seed=0",
             "n_pcfs": n, "pairs_per_step": n * (n - 1) // 2,
             "output": "condensed DistanceMatrix float32 kept in HBM",
             "l2": "inputs (CSR) and output larger than L2; no flush",
+            "processing_order": "caller" if getattr(args, "order", 0) == 1 else "length order in 1024-PCF windows",
+            "generator_sha256": _generator_hash(),
             "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
 
 
