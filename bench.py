@@ -356,7 +356,7 @@ def run_reference(args, ws, rank):
         return
     pts, off = workload(args.n, seed=0)
     threads = os.cpu_count() or 1
-    rows = sample_rows(args.n, 2.0e6 if args.n >= 50_000 else args.n * (args.n - 1) / 2)
+    rows = sample_rows(args.n, min(2.0e6, args.n * (args.n - 1) / 2))
     for _ in range(args.warmup):
         cpu_baseline(pts, off, rows[: max(1, len(rows) // 8)], threads)
     rates, times, pairs_tot = [], [], 0
