@@ -62,6 +62,23 @@ namespace sbg
     }
   }
 
+  // blk + (tn - t) * op(f, g) for a rectangle of positive width; a
+  // zero-width rectangle (the row advancing alone on a tie) adds nothing, as
+  // in the reference, whose merge advances both sides on a tie and never
+  // forms one (so an infinite value there gives inf, not inf * 0 = NaN).
+  // Times never decrease along the merge, so tn == t means width zero; for
+  // double the test runs on the bit patterns (integer pipe).
+  template <int K>
+  __device__ __forceinline__ float accumulate(float blk, float t, float tn, float f, float g, float p)
+  {
+    return tn == t ? blk : PairOp<K>::acc(blk, tn - t, f, g, p);
+  }
+  template <int K>
+  __device__ __forceinline__ double accumulate(double blk, double t, double tn, double f, double g, double p)
+  {
+    return __double_as_longlong(tn) == __double_as_longlong(t) ? blk : PairOp<K>::acc(blk, tn - t, f, g, p);
+  }
+
   // The merge of one row (warp-shared, segment layout at pf) against one
   // column per lane (segment layout at pg, stride GS elements between
   // consecutive elements of the same column).  `steps` is warp-uniform.
@@ -84,7 +101,7 @@ namespace sbg
       {
         const bool takeF = row_first(F.tn, G.tn);
         const T tn = takeF ? F.tn : G.tn;
-        blk = PairOp<K>::acc(blk, tn - t, F.v, G.v, p);
+        blk = accumulate<K>(blk, t, tn, F.v, G.v, p);
         t = tn;
         if (FCLAMP)
         {
@@ -194,7 +211,7 @@ namespace sbg
       for (int u = 0; u < U; ++u)
       {
         const T tn = earlier(ft, G.tn);
-        blk = PairOp<K>::acc(blk, tn - t, fv, G.v, p);
+        blk = accumulate<K>(blk, t, tn, fv, G.v, p);
         t = tn;
         advance_shared_soa(fv, ft, G.v, G.tn, af, voff, ag);
       }
@@ -221,7 +238,7 @@ namespace sbg
       for (int u = 0; u < U; ++u)
       {
         const T tn = earlier(F.tn, G.tn);
-        blk = PairOp<K>::acc(blk, tn - t, F.v, G.v, p);
+        blk = accumulate<K>(blk, t, tn, F.v, G.v, p);
         t = tn;
         advance_shared(F.v, F.tn, G.v, G.tn, af, ag);
       }
@@ -465,7 +482,7 @@ namespace sbg
       for (int u = 0; u < U; ++u)
       {
         const T tn = earlier(F.tn, G.tn);
-        blk = PairOp<K>::acc(blk, tn - t, F.v, G.v, p);
+        blk = accumulate<K>(blk, t, tn, F.v, G.v, p);
         t = tn;
         advance_hybrid(F.v, F.tn, G.v, G.tn, row, fi, flast, ag);
       }

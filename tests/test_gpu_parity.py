@@ -467,3 +467,23 @@ def test_device_bands_of_whole_windows_use_the_length_order():
         parts.append(buf)
     torch.cuda.synchronize()
     assert torch.equal(torch.cat(parts), whole)
+
+
+def test_infinite_values_at_shared_breakpoints():
+    """A value of inf right after a breakpoint both PCFs share: the
+    reference advances both sides there and returns inf; no zero-width
+    rectangle may turn it into inf * 0 = NaN."""
+    import stablebear_gb300 as sb
+    from oracle import oracle as orc
+    for dt in (np.float32, np.float64):
+        pcfs = [[[0, 0], [1, np.inf], [2, 0]], [[0, 0], [1, 5], [3, 0]], [[0, 1], [1, 2], [2, 0]],
+                [[0, -np.inf], [1, 0]], [[0, 0], [1, 0]]]
+        pts = np.concatenate([np.array(p, dt) for p in pcfs])
+        off = np.zeros(len(pcfs) + 1, np.uint64)
+        np.cumsum([len(p) for p in pcfs], out=off[1:])
+        X = arr(pts, off)
+        for got, op, mode in ((sb.pdist(X).data, orc.OP_L1, orc.MODE_PDIST),
+                              (sb.l2_kernel(X).data, orc.OP_L2, orc.MODE_KERNEL)):
+            want = orc.evaluate(pts, off, op=op, mode=mode)
+            np.testing.assert_array_equal(np.isnan(got), np.isnan(want))
+            np.testing.assert_array_equal(got[np.isinf(want)], want[np.isinf(want)])
