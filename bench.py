@@ -74,6 +74,21 @@ def _device_problem(pts, off):
     return torch.from_numpy(pts).cuda(), torch.from_numpy(off.astype(np.int64)).cuda()
 
 
+def _traffic_per_launch(kernel, n):
+    """DRAM bytes (read + write) per launch from the committed ncu capture
+    ``profiles/traffic.json``, scaled from the captured case by output pairs
+    (the traffic is the condensed output stream); None without a capture."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "traffic.json")
+    try:
+        with open(path) as fh:
+            e = json.load(fh).get(kernel)
+    except (OSError, ValueError):
+        return None
+    if not e:
+        return None
+    return float(e["bytes"]) * (n * (n - 1) // 2) / float(e["pairs"])
+
+
 def _hbm_peak():
     """HBM copy bandwidth (GB/s) measured on the GB300s, else the
     earlier single measurement."""
@@ -523,7 +538,7 @@ def main():
     from stablebear_gb300 import roofline
     peak = roofline.fp32_peak(local)
     achieved = segs * W_SEG / (ms_step / 1e3) / 1e12
-    traffic = roofline.traffic_per_launch("pairs_kernel_l1_f32", n)
+    traffic = _traffic_per_launch("pairs_kernel_l1_f32", n)
     # The pipe that actually bounds the kernel: every merged rectangle brings
     # one new 8-byte (t, v) element per lane out of shared memory; the peak is
     # 128 B per clock per SM at the sampled SM clock.
