@@ -12,7 +12,8 @@
 //   * a launch is one queue reset plus one kernel; with SBG_BATCH_GRAPH the
 //     pair is captured once into a CUDA graph and replayed;
 //   * sbg_batch_autotune times a few (warps per CTA, rows per item)
-//     settings on the real batch and keeps the fastest.
+//     settings on the real batch, then a few sizes of the shared column
+//     block, and keeps the fastest.
 #include "../../include/sbgpu.h"
 #include "sbg_internal.hpp"
 
@@ -153,7 +154,27 @@ namespace sbg
         }
       }
       rebuild_items(bw, bs);
+      // Column groups longer than the staging block read their columns
+      // through L1; a smaller block leaves more of the SM's unified
+      // L1/shared memory to the rows, which are always read through L1.
+      const uint32_t full = pl.lmax_c;
+      uint32_t bc = full;
+      for (uint32_t c : {full / 2, full / 4})
+      {
+        if (c < 32) continue;
+        set_column_block(c);
+        const double ms = time_once(st, 2);
+        if (ms < best) { best = ms; bc = c; }
+      }
+      set_column_block(bc);
       return best;
+    }
+
+    void set_column_block(uint32_t cap)
+    {
+      pl.lmax_c = cap;
+      pl.smem_bytes = (size_t)32 * cap * sizeof(Elem<T>);
+      drop_graph();
     }
 
     void info(uint64_t* items, uint64_t* pairs, int* warps, int* rows_per_item) const override
