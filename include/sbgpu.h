@@ -283,6 +283,19 @@ uint64_t sbg_kernel_launches(void);
 /* Number of output elements of a problem (n(n-1)/2, n(n+1)/2 or n_rows*n_cols). */
 uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols);
 
+/* One scheduler block of the output: the dense row_height x col_width tile of
+ * rows [row_start, row_start + row_height) against columns [col_start,
+ * col_start + col_width), row-major with stride col_width, into a device
+ * matrix the caller has cleared.  Entries the skip mode excludes (global
+ * column > row, or >= row without the diagonal) are left zero.  Row and
+ * column CSRs may be the same (pdist, kernel) or different (cdist); their
+ * offsets are absolute into their points.  Device pointers, caller's stream.
+ * Replaces PcfBlockOp::exec_block (include/sbear/cuda/pcf_block_op.cuh:82-122). */
+int sbg_block_device(int dtype, int op, double p, int skip_mode, const void* row_points,
+                     const uint64_t* row_offsets, const void* col_points, const uint64_t* col_offsets,
+                     uint64_t row_start, uint64_t row_height, uint64_t col_start, uint64_t col_width,
+                     uint32_t max_points, void* tile, void* stream);
+
 /* ---- device-resident result containers ------------------------------------ */
 
 /* Dense rows [row_begin, row_end) of the n x n matrix held in condensed form

@@ -77,6 +77,7 @@ SIGNATURES = {
     "sbg_batch_destroy": (None, [_P]),
     "sbg_output_count": (_U64, [_I, _U64, _U64]),
     "sbg_kernel_launches": (_U64, []),
+    "sbg_block_device": (_I, [_I, _I, _D, _I, _P, _P, _P, _P, _U64, _U64, _U64, _U64, ctypes.c_uint32, _P, _P]),
     "sbg_length_order_device": (_I, [_P, _U64, _P, _P]),
     "sbg_measure_peak": (_I, [_I, ctypes.POINTER(_D)]),
     "sbg_enumerate_items": (_U64, [_I, _U64, _U64, _U64, _U64, ctypes.c_uint32, _P, _U64]),

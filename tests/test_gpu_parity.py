@@ -206,7 +206,9 @@ def test_variants_orders_and_bands_agree():
     np.testing.assert_array_equal(gm, base)
     np.testing.assert_array_equal(banded, base)
     np.testing.assert_array_equal(small, base)
-    assert rel_err(srt, base) <= 1e-5
+    # zero-width rectangles add nothing, so neither the processing order nor
+    # which PCF of a pair is the warp's row changes a bit of the result
+    np.testing.assert_array_equal(srt, base)
 
 
 def test_long_pcfs_use_global_memory_path():
