@@ -233,12 +233,14 @@ namespace sbg
     }
 
     // Rows per item = 32 q: as large as possible (fewer column reloads,
-    // less end-of-item idling) while keeping >= 6 items per SM.
+    // less end-of-item idling) while keeping >= 6 items per SM.  At most
+    // 1024 rows, one processing-order window, so that bands of whole
+    // windows start on item boundaries.
     uint32_t q = (uint32_t)std::max(0, settings().rowChunk.load());
     if (q == 0)
     {
       q = 1;
-      for (uint32_t cand = 16; cand >= 1; cand /= 2)
+      for (uint32_t cand = 32; cand >= 1; cand /= 2)
       {
         if (items_for(mode, 0, nr, nc, cand) >= (uint64_t)dev.sms * 6) { q = cand; break; }
       }
