@@ -54,6 +54,16 @@ def test_argument_errors_need_no_device(lib):
     assert lib.sbg_create_integrate_task(0, 0, 1.0, 0, P(pts), P(off), 2, P(out), ctypes.byref(h)) == -1
     assert lib.sbg_set_tuning(99, 0, 0, 0, 0) == -1
     assert lib.sbg_set_block_dim(0, 1) == -1
+    # the newer entries check their arguments before any CUDA call
+    assert lib.sbg_block_device(7, 0, 1.0, 1, None, None, None, None, 0, 4, 0, 4, 8, None, None) == -1
+    assert lib.sbg_block_device(0, 1, 0.5, 1, None, None, None, None, 0, 4, 0, 4, 8, None, None) == -1
+    assert b"p must be >= 1" in lib.sbg_last_error()
+    assert lib.sbg_block_device(0, 0, 1.0, 1, None, None, None, None, 0, 4, 0, 4, 8, None, None) == -1
+    assert b"null pointer" in lib.sbg_last_error()
+    assert lib.sbg_lp_norm_host(0, 0.5, P(pts), P(off), 2, P(out)) == -1
+    assert lib.sbg_condensed_to_dense_device(0, 0, 4, None, None, 4, 0, 4, None) == -1  # cdist storage is not condensed
+    assert lib.sbg_barcodes_to_pcfs_host(5, 0, None, None, 0, None, 0, None) == -1
+    assert lib.sbg_barcode_pcf_capacity(0, 3, 10) == 13 and lib.sbg_barcode_pcf_capacity(1, 3, 10) == 23
 
 
 def test_invalid_pcf_input_rejected_before_device(lib):
