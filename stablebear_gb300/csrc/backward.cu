@@ -100,7 +100,7 @@ namespace sbg
   }
 
   template <typename T, int OP, bool SQUARE, bool WARP_ITEMS>
-  __global__ void __launch_bounds__(512) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
+  __global__ void __launch_bounds__(1024) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
   {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sgrad_all = reinterpret_cast<T*>(smem_raw);
@@ -195,30 +195,31 @@ namespace sbg
             seg_coeffs<OP>(F.v, Gc.v, cf, cg);
             accF = fma(dt, cf, accF);
             accG = fma(dt, cg, accG);
-            if (takeF)
+            // Which side moves on; the row stays on its last element once
+            // exhausted (it then runs to TMAX).  Gc.tn < F.tn <= TMAX when the
+            // column moves, so the column has a next element.  The loads and
+            // adds are predicated rather than branched, so the lanes of a
+            // warp do not split into the two sides' paths.
+            const bool advF = takeF && fi + 1 < rlen;
+            const bool advG = !takeF;
+            Elem<T> Fn = F, Gn = Gc;
+            if (advF) Fn = row[fi + 1];
+            if (advG) Gn = col[gi + 1];
+            if (w != T(0))
             {
-              if (fi + 1 < rlen)
-              {
-                if (w != T(0)) atomicAdd(&sg[2 * fi], w * accF);
-                accF = T(0);
-                const Elem<T> Fn = row[fi + 1];
-                if (w != T(0) && !(F.tn == Gc.tn)) atomicAdd(&sg[2 * fi + 1], w * step_delta<OP>(F.v, Fn.v, Gc.v));
-                ++fi;
-                F = Fn;
-              }
-            }
-            else
-            {
-              // Gc.tn < F.tn <= TMAX, so the column has a next element:
-              // dL/dv of this element and dL/dt of the next share a slot
-              const Elem<T> Gn = col[gi + 1];
-              if (!SQUARE && w != T(0))
+              if (advF) atomicAdd(&sg[2 * fi], w * accF);
+              if (advF && !(F.tn == Gc.tn)) atomicAdd(&sg[2 * fi + 1], w * step_delta<OP>(F.v, Fn.v, Gc.v));
+              // dL/dv of the column element and dL/dt of the next share a slot
+              if (!SQUARE && advG)
                 red_add2(&B.grad[2 * (coff + gi)], w * accG,
                          (Gc.tn == t) ? T(0) : w * step_delta<OP>(Gc.v, Gn.v, F.v));
-              accG = T(0);
-              ++gi;
-              Gc = Gn;
             }
+            accF = advF ? T(0) : accF;
+            accG = advG ? T(0) : accG;
+            fi += advF ? 1u : 0u;
+            gi += advG ? 1u : 0u;
+            F = Fn;
+            Gc = Gn;
             t = tn;
           }
           if (w != T(0)) atomicAdd(&sg[2 * fi], w * accF);
@@ -322,7 +323,10 @@ namespace sbg
     B.grad_out = grad_out; B.fwd = fwd; B.grad = static_cast<T*>(paired);
     B.queue = static_cast<unsigned long long*>(queue);
     B.row_cap = lmax;
-    const int warps = 16;
+    // As many warps (up to 32) as the per-warp row-gradient buffers allow:
+    // the merge is latency-bound, so occupancy pays.
+    int warps = 32;
+    while (warps > 1 && (size_t)warps * lmax * 2 * sizeof(T) + 2048 > dev.smem_optin) warps /= 2;
     const size_t smem = (size_t)warps * lmax * 2 * sizeof(T);
     if (smem + 2048 > dev.smem_optin) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
     // The ordered-pairs variant measured slower on GB300 (N = 4096, L2 kernel:
