@@ -48,6 +48,7 @@ namespace sbg
     const T* fwd;           // condensed M (distances), or null
     T* grad;                // (npts, 2): [dL/dt, dL/dv]
     uint32_t row_cap;       // per-warp shared gradient buffer (elements)
+    uint32_t cols_cap;      // staged column elements per lane (0: columns read through L1)
   };
 
   namespace
@@ -102,8 +103,13 @@ namespace sbg
   template <typename T, int OP, bool SQUARE, bool WARP_ITEMS>
   __global__ void __launch_bounds__(1024) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
   {
+    // Shared memory: the item's 32 columns, interleaved (element k of column
+    // j at [k * 32 + j]) when cols_cap > 0, then the per-warp row-gradient
+    // buffers.
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sgrad_all = reinterpret_cast<T*>(smem_raw);
+    Elem<T>* cols = reinterpret_cast<Elem<T>*>(smem_raw);
+    T* sgrad_all = reinterpret_cast<T*>(cols + (size_t)B.cols_cap * 32);
+    const int nwarps = blockDim.x >> 5;
     __shared__ unsigned long long s_item;
     __shared__ unsigned int s_next_row;
     const int lane = threadIdx.x & 31;
@@ -147,6 +153,17 @@ namespace sbg
       const uint32_t clen = (uint32_t)(B.off[cj_eff + 1] - coff);
       const uint32_t maxlc = __reduce_max_sync(FULL, clen);
       const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > B.npts);
+      // the same item for every warp: these are CTA-uniform
+      const bool staged = !WARP_ITEMS && B.cols_cap > 0 && item_ok && maxlc <= B.cols_cap;
+      if (!WARP_ITEMS && B.cols_cap > 0)
+      {
+        if (staged)
+          for (uint32_t k = warp; k < maxlc; k += nwarps)
+            if (k < clen) cols[(size_t)k * 32 + lane] = B.pk[coff + k];
+        __syncthreads();
+      }
+      const Elem<T>* colbase = staged ? cols + lane : B.pk + coff;
+      const uint32_t cstride = staged ? 32u : 1u;
 
       if (item_ok)
       {
@@ -181,8 +198,7 @@ namespace sbg
           __syncwarp();
 
           const Elem<T>* row = B.pk + roff;
-          const Elem<T>* col = B.pk + coff;
-          Elem<T> F = row[0], Gc = col[0];
+          Elem<T> F = row[0], Gc = colbase[0];
           uint32_t fi = 0, gi = 0;
           T t = T(0), accF = T(0), accG = T(0);
           const uint32_t steps = rlen + maxlc - 1;
@@ -204,7 +220,7 @@ namespace sbg
             const bool advG = !takeF;
             Elem<T> Fn = F, Gn = Gc;
             if (advF) Fn = row[fi + 1];
-            if (advG) Gn = col[gi + 1];
+            if (advG) Gn = colbase[(size_t)(gi + 1) * cstride];
             if (w != T(0))
             {
               if (advF) atomicAdd(&sg[2 * fi], w * accF);
@@ -323,12 +339,25 @@ namespace sbg
     B.grad_out = grad_out; B.fwd = fwd; B.grad = static_cast<T*>(paired);
     B.queue = static_cast<unsigned long long*>(queue);
     B.row_cap = lmax;
-    // As many warps (up to 32) as the per-warp row-gradient buffers allow:
-    // the merge is latency-bound, so occupancy pays.
+    // The item's columns are staged in shared memory when that still leaves
+    // room for 16 warps' row-gradient buffers; otherwise they are read
+    // through L1.  Then as many warps (up to 32) as fit: the merge is
+    // latency-bound, so occupancy pays.
+    const size_t grad_per_warp = (size_t)lmax * 2 * sizeof(T);
+    const size_t cols_bytes = (size_t)32 * lmax * sizeof(Elem<T>);
+    const size_t budget = dev.smem_optin > 2048 ? dev.smem_optin - 2048 : 0;
+#ifdef SBG_BWD_WARP_ITEMS
+    const bool stage = false;
+#else
+    const bool stage = cols_bytes + 16 * grad_per_warp <= budget;
+#endif
+    B.cols_cap = stage ? lmax : 0;
+    const size_t fixed = stage ? cols_bytes : 0;
     int warps = 32;
-    while (warps > 1 && (size_t)warps * lmax * 2 * sizeof(T) + 2048 > dev.smem_optin) warps /= 2;
-    const size_t smem = (size_t)warps * lmax * 2 * sizeof(T);
-    if (smem + 2048 > dev.smem_optin) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
+    while (warps > 1 && fixed + (size_t)warps * grad_per_warp > budget) warps /= 2;
+    if (stage) while (warps < 32 && fixed + (size_t)(warps + 8) * grad_per_warp <= budget) warps += 8;
+    const size_t smem = fixed + (size_t)warps * grad_per_warp;
+    if (smem > budget) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
     // The ordered-pairs variant measured slower on GB300 (N = 4096, L2 kernel:
     // forward + backward 74 ms against 46 ms): twice the merges, and the
     // lanes' shared-memory adds into one row buffer contend.  It stays
