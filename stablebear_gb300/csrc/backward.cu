@@ -339,17 +339,19 @@ namespace sbg
     B.grad_out = grad_out; B.fwd = fwd; B.grad = static_cast<T*>(paired);
     B.queue = static_cast<unsigned long long*>(queue);
     B.row_cap = lmax;
-    // The item's columns are staged in shared memory when that still leaves
-    // room for 16 warps' row-gradient buffers; otherwise they are read
-    // through L1.  Then as many warps (up to 32) as fit: the merge is
-    // latency-bound, so occupancy pays.
+    // As many warps (up to 32) as the per-warp row-gradient buffers allow:
+    // the merge is latency-bound, so occupancy pays.  Columns are read
+    // through L1: staging them in shared memory (behind
+    // SBG_BWD_STAGE_COLUMNS) costs warps and measured slower (N = 4096, L2
+    // kernel, forward + backward: 26.4 ms with 24 warps and staged columns
+    // against 25.6 ms with 32 warps).
     const size_t grad_per_warp = (size_t)lmax * 2 * sizeof(T);
     const size_t cols_bytes = (size_t)32 * lmax * sizeof(Elem<T>);
     const size_t budget = dev.smem_optin > 2048 ? dev.smem_optin - 2048 : 0;
-#ifdef SBG_BWD_WARP_ITEMS
-    const bool stage = false;
-#else
+#if defined(SBG_BWD_STAGE_COLUMNS) && !defined(SBG_BWD_WARP_ITEMS)
     const bool stage = cols_bytes + 16 * grad_per_warp <= budget;
+#else
+    const bool stage = false;
 #endif
     B.cols_cap = stage ? lmax : 0;
     const size_t fixed = stage ? cols_bytes : 0;
