@@ -114,7 +114,10 @@ namespace sbg
     __shared__ unsigned int s_next_row;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    T* sg = sgrad_all + (size_t)warp * B.row_cap * 2;  // slot k: dL/dv_k, dL/dt_{k+1}
+    // per warp: dL/dv_k at sgv[k], dL/dt_{k+1} at sgt[k] (two arrays: lanes at
+    // nearby row positions then hit distinct banks)
+    T* sgv = sgrad_all + (size_t)warp * B.row_cap * 2;
+    T* sgt = sgv + B.row_cap;
     const unsigned FULL = 0xffffffffu;
 
     for (;;)
@@ -194,7 +197,7 @@ namespace sbg
           }
           if (!__any_sync(FULL, w != T(0))) continue;
 
-          for (uint32_t k = lane; k < rlen; k += 32) { sg[2 * k] = T(0); sg[2 * k + 1] = T(0); }
+          for (uint32_t k = lane; k < rlen; k += 32) { sgv[k] = T(0); sgt[k] = T(0); }
           __syncwarp();
 
           const Elem<T>* row = B.pk + roff;
@@ -223,8 +226,8 @@ namespace sbg
             if (advG) Gn = colbase[(size_t)(gi + 1) * cstride];
             if (w != T(0))
             {
-              if (advF) atomicAdd(&sg[2 * fi], w * accF);
-              if (advF && !(F.tn == Gc.tn)) atomicAdd(&sg[2 * fi + 1], w * step_delta<OP>(F.v, Fn.v, Gc.v));
+              if (advF) atomicAdd(&sgv[fi], w * accF);
+              if (advF && !(F.tn == Gc.tn)) atomicAdd(&sgt[fi], w * step_delta<OP>(F.v, Fn.v, Gc.v));
               // dL/dv of the column element and dL/dt of the next share a slot
               if (!SQUARE && advG)
                 red_add2(&B.grad[2 * (coff + gi)], w * accG,
@@ -238,12 +241,12 @@ namespace sbg
             Gc = Gn;
             t = tn;
           }
-          if (w != T(0)) atomicAdd(&sg[2 * fi], w * accF);
+          if (w != T(0)) atomicAdd(&sgv[fi], w * accF);
           if (!SQUARE && w != T(0)) atomicAdd(&B.grad[2 * (coff + gi)], w * accG);
           __syncwarp();
           for (uint32_t k = lane; k < rlen; k += 32)
           {
-            const T gv = sg[2 * k], gt = sg[2 * k + 1];
+            const T gv = sgv[k], gt = sgt[k];
             if (gv != T(0) || gt != T(0)) red_add2(&B.grad[2 * (roff + k)], gv, gt);
           }
           __syncwarp();
