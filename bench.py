@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--order", type=int, default=0, choices=[0, 1],
                     help="processing order of the device entry: 0 length order (default), 1 caller order")
+    ap.add_argument("--variant", type=int, default=0, choices=range(0, 7),
+                    help="kernel variant of the engine (0 automatic; 4 hybrid, 5 shared memory, 6 time-windowed)")
     ap.add_argument("--config", default="large",
                     choices=["large", "plain", "stable_rank", "batched", "fwdbwd", "dense"],
                     help="large: the headline workload; the others print their own report line")
@@ -108,6 +110,9 @@ def run_aux(args):
     st = lambda: ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     threads = os.cpu_count() or 1
     rep = {"config_name": args.config, "data": "synthetic"}
+    if args.variant:
+        nat.check(lib.sbg_set_tuning(0, 0, args.variant, 0, 0))
+        rep["variant"] = args.variant
 
     def single(pts, off, opc, p, skip, out, lmax):
         dp, do = _device_problem(pts, off)
@@ -432,8 +437,8 @@ def main():
     sptr = ctypes.c_void_p(stream.cuda_stream)
     lib = nat.lib()
 
-    if args.order:
-        sb.set_tuning(order=args.order)
+    if args.order or args.variant:
+        sb.set_tuning(order=args.order, variant=args.variant)
 
     def step():
         nat.check(lib.sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),

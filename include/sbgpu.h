@@ -93,10 +93,19 @@ int sbg_get_device_verbose(void);
  * variant (1 shared-memory with 8-byte row elements, 2 global-memory, 3
  * shared-memory with a two-load walk, 4 hybrid: columns in shared memory,
  * rows read through L1, 5 shared-memory with the row as separate time and
- * value arrays, the automatic choice when the PCFs fit), order
+ * value arrays, the automatic choice when the PCFs fit, 6 time-windowed
+ * shared memory: each work item walks time windows holding at most a cap of
+ * elements of every PCF, the automatic choice for longer PCFs), order
  * (1 caller's, 2 sorted
  * by breakpoint count), output bytes per pipeline band. */
 int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes);
+
+/* Time-windowed variant: the most elements of one PCF inside a window
+ * (0 = the most that fit in shared memory).  SBG_ERR_INVALID_ARGUMENT
+ * outside [0, 1048576]; a cap too large for shared memory fails the call
+ * that plans with it. */
+int sbg_set_window_cap(int cap);
+int sbg_get_window_cap(void);
 
 /* How host-buffer entry points return results: 0 automatic (= 1), 1 device
  * bands copied out through pinned staging buffers while the next band

@@ -15,7 +15,7 @@ from .distance import (
 )
 from .system import (
     force_cpu, set_block_size, limit_cpus, limit_gpus, set_cuda_threshold, get_cuda_threshold,
-    set_device_verbose, set_min_block_side, set_tuning, build_type, get_ngpus,
+    set_device_verbose, set_min_block_side, set_tuning, set_window_cap, get_window_cap, build_type, get_ngpus,
 )
 from .task import StoppableTask, EmptyTask
 from .io import save, load
@@ -28,8 +28,8 @@ __all__ = [
     "pdist", "cdist", "l2_kernel", "lp_distance",
     "Distance_f32_f32", "Distance_f64_f64", "InnerProduct_f32_f32", "InnerProduct_f64_f64",
     "force_cpu", "set_block_size", "limit_cpus", "limit_gpus", "set_cuda_threshold", "get_cuda_threshold",
-    "set_device_verbose", "set_min_block_side", "set_tuning", "build_type", "get_ngpus",
-    "StoppableTask", "EmptyTask", "save", "load", "lp_norm", "Norms_f32_f32", "Norms_f64_f64",
+    "set_device_verbose", "set_min_block_side", "set_tuning", "set_window_cap", "get_window_cap", "build_type",
+    "get_ngpus", "StoppableTask", "EmptyTask", "save", "load", "lp_norm", "Norms_f32_f32", "Norms_f64_f64",
     "persistence",
 ]
 

@@ -53,6 +53,8 @@ SIGNATURES = {
     "sbg_get_device_verbose": (_I, []),
     "sbg_set_tuning": (_I, [_I, _I, _I, _I, _U64]),
     "sbg_set_output_mode": (_I, [_I]),
+    "sbg_set_window_cap": (_I, [_I]),
+    "sbg_get_window_cap": (_I, []),
     "sbg_host_memory_access": (_I, [ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "sbg_create_integrate_task": (_I, [_I, _I, _D, _I, _P, _P, _U64, _P, ctypes.POINTER(_P)]),
     "sbg_create_cdist_task": (_I, [_I, _I, _D, _P, _P, _U64, _P, _P, _U64, _P, ctypes.POINTER(_P)]),

@@ -49,6 +49,11 @@ namespace sbg
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     uint64_t graph_kernels = 0;  // kernels one replay of the graph runs
+    bool windowed = false;       // time-windowed kernel (else the hybrid one)
+    uint32_t lmax = 1;           // longest PCF of the batch
+    size_t usable = 0;           // shared memory per CTA
+    uint32_t win_cap = 0;        // slice cap, fixed for the batch: window ends (and so the
+                                 // rounding of every sum) do not change with the autotuned shape
 
     ~Batch() override { drop_graph(); }
 
@@ -58,8 +63,20 @@ namespace sbg
       if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
     }
 
-    void rebuild_items(uint32_t warps, uint32_t qscale)
+    // Rows per item and warps; the time-windowed layout depends on both.
+    // False (and nothing changed) when that layout does not fit.
+    bool rebuild_items(uint32_t warps, uint32_t qscale)
     {
+      if (windowed)
+      {
+        uint64_t qmax = 1;
+        for (size_t k = 0; k < descs.size(); ++k) qmax = std::max<uint64_t>(qmax, q_base[k] * qscale);
+        Plan trial = pl;
+        if (qmax > 1024 ||
+            !window_layout(trial, sizeof(Elem<T>), (int)warps, (uint32_t)(32 * qmax), lmax, usable, win_cap))
+          return false;
+        pl = trial;
+      }
       uint64_t begin = 0;
       for (size_t k = 0; k < descs.size(); ++k)
       {
@@ -73,6 +90,7 @@ namespace sbg
       q_scale = qscale;
       SBG_CUDA(cudaMemcpy(d_descs.get(), descs.data(), sizeof(ProblemDesc<T>) * descs.size(), cudaMemcpyHostToDevice));
       drop_graph();
+      return true;
     }
 
     void enqueue(cudaStream_t st)
@@ -86,6 +104,8 @@ namespace sbg
       L.queue = d_queue.as<unsigned long long>();
       L.lmax_c = pl.lmax_c;
       L.row_cap = pl.row_cap;
+      L.win_r = pl.win_r;
+      L.row_slots = pl.row_slots;
       const int grid = (int)std::min<uint64_t>((uint64_t)dev.sms, total_items);
       SBG_CUDA(launch_pairs<T>(L, opk, pl.kvar, pl.warps, grid, pl.smem_bytes, st));
     }
@@ -148,15 +168,16 @@ namespace sbg
       {
         for (uint32_t s : scale_c)
         {
-          rebuild_items(w, s);
+          if (!rebuild_items(w, s)) continue;
           const double ms = time_once(st, 2);
           if (ms < best) { best = ms; bw = w; bs = s; }
         }
       }
-      rebuild_items(bw, bs);
-      // Column groups longer than the staging block read their columns
-      // through L1; a smaller block leaves more of the SM's unified
-      // L1/shared memory to the rows, which are always read through L1.
+      if (!rebuild_items(bw, bs)) throw Error(ST_INTERNAL, "batch autotune: the chosen layout no longer fits");
+      if (windowed) return best;
+      // Hybrid kernel: column groups longer than the staging block read
+      // their columns through L1; a smaller block leaves more of the SM's
+      // unified L1/shared memory to the rows, which are always read through L1.
       const uint32_t full = pl.lmax_c;
       uint32_t bc = full;
       for (uint32_t c : {full / 2, full / 4})
@@ -194,6 +215,10 @@ namespace sbg
     b->use_graph = (flags & SBG_BATCH_GRAPH) != 0;
     b->dev = device_info();
     const bool sort_len = (flags & SBG_BATCH_CALLER_ORDER) == 0;
+    // the time-windowed kernel for float (the hybrid one on request), the
+    // hybrid one for double (FP64-bound either way; it measured faster)
+    const int var = settings().variant.load();
+    b->windowed = var == 6 || (var != 4 && sizeof(T) == 4);
 
     // Host copies of the offsets (given, or read back once).
     std::vector<std::vector<uint64_t>> hoff(n);
@@ -219,7 +244,7 @@ namespace sbg
 
     // Length permutations and packed layouts, concatenated.
     b->d_perm.reset(std::max<uint64_t>(1, tot_n) * sizeof(uint32_t));
-    b->d_packed.reset(std::max<uint64_t>(1, tot_pts) * sizeof(Elem<T>));
+    if (!b->windowed) b->d_packed.reset(std::max<uint64_t>(1, tot_pts) * sizeof(Elem<T>));
     std::vector<uint32_t> hperm(tot_n);
     uint64_t pbase = 0, ebase = 0;
     struct Pending { ProblemDesc<T> d; double cost; uint64_t qb; };
@@ -233,11 +258,15 @@ namespace sbg
       const uint64_t* o = hoff[k].data();
       if (sort_len)
         std::stable_sort(hp, hp + P.n, [o](uint32_t a, uint32_t c) { return (o[a + 1] - o[a]) < (o[c + 1] - o[c]); });
-      Elem<T>* packed = b->d_packed.template as<Elem<T>>() + ebase;
-      SBG_CUDA(launch_pack<T>(static_cast<const T*>(P.points), P.offsets, P.n, packed, o[P.n], b->dev.sms, 0));
-
       ProblemDesc<T> d{};
-      d.rpts = reinterpret_cast<const T*>(packed); d.roff = P.offsets; d.nr = P.n;
+      if (b->windowed) d.rpts = static_cast<const T*>(P.points);  // the CSR itself
+      else
+      {
+        Elem<T>* packed = b->d_packed.template as<Elem<T>>() + ebase;
+        SBG_CUDA(launch_pack<T>(static_cast<const T*>(P.points), P.offsets, P.n, packed, o[P.n], b->dev.sms, 0));
+        d.rpts = reinterpret_cast<const T*>(packed);
+      }
+      d.roff = P.offsets; d.nr = P.n;
       d.cpts = d.rpts; d.coff = P.offsets; d.nc = P.n;
       d.rperm = sort_len ? b->d_perm.template as<uint32_t>() + pbase : nullptr;
       d.cperm = d.rperm;
@@ -264,28 +293,49 @@ namespace sbg
       b->q_base.push_back(x.qb);
     }
 
-    // One plan for the whole batch: the hybrid kernel (columns in shared
-    // memory when a group fits, rows through L1) reads the packed layout.
+    // One plan for the whole batch: the time-windowed kernel on the CSR
+    // (windows only where PCFs are long), or on request the hybrid kernel
+    // (columns in shared memory when a group fits, rows through L1) on the
+    // packed layout.
     Plan pl;
+    const size_t es = sizeof(Elem<T>);
+    b->usable = b->dev.smem_optin > 2048 ? b->dev.smem_optin - 2048 : 0;
+    b->lmax = lmax;
+    const int want_w = settings().warps.load();
+    pl.smem = true;
+    pl.q = 1;
+    pl.grid = b->dev.sms;
+    if (b->windowed)
     {
-      const size_t es = sizeof(Elem<T>);
-      const size_t usable = b->dev.smem_optin > 2048 ? b->dev.smem_optin - 2048 : 0;
-      const int want_w = settings().warps.load();
-      pl.smem = true;
+      pl.packed = false;
+      pl.kvar = 6;
+      pl.warps = want_w > 0 ? std::min(want_w, 32) : 24;
+      // One cap for every shape the autotune tries (up to 32 warps and 4x
+      // the rows per item), else the one that fits the starting shape.
+      uint64_t qb = 1;
+      for (uint64_t x : b->q_base) qb = std::max(qb, x);
+      Plan probe;
+      if (window_layout(probe, es, 32, (uint32_t)(32 * qb * 4), lmax, b->usable))
+        b->win_cap = probe.lmax_c;
+      else if (window_layout(probe, es, pl.warps, (uint32_t)(32 * qb), lmax, b->usable))
+        b->win_cap = probe.lmax_c;
+    }
+    else
+    {
       pl.packed = true;
       pl.kvar = 3;
       pl.warps = want_w > 0 ? std::min(want_w, 32) : 32;
-      pl.lmax_c = (uint32_t)std::min<size_t>(lmax, usable / (32 * es));
+      pl.lmax_c = (uint32_t)std::min<size_t>(lmax, b->usable / (32 * es));
       pl.row_cap = 0;
       pl.smem_bytes = (size_t)32 * pl.lmax_c * es;
-      pl.q = 1;
-      pl.grid = b->dev.sms;
     }
     b->pl = pl;
     b->d_descs.reset(std::max<size_t>(1, b->descs.size()) * sizeof(ProblemDesc<T>));
     b->d_queue.reset(256);
     SBG_CUDA(cudaDeviceSynchronize());
-    b->rebuild_items((uint32_t)pl.warps, 1);
+    bool fit = false;
+    for (int w = pl.warps; w >= 4 && !fit; w -= 4) fit = b->rebuild_items((uint32_t)w, 1);
+    if (!fit) throw Error(ST_INVALID_ARGUMENT, "batch: the window setting does not fit in shared memory");
     return b.release();
   }
 }

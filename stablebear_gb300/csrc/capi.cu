@@ -202,7 +202,7 @@ extern "C"
     return guarded([&] {
       if (warps < 0 || warps > 32) throw Error(ST_INVALID_ARGUMENT, "warps must be in [0, 32]");
       if (row_chunk < 0 || row_chunk > 1024) throw Error(ST_INVALID_ARGUMENT, "row_chunk must be in [0, 1024]");
-      if (variant < 0 || variant > 5) throw Error(ST_INVALID_ARGUMENT, "variant must be in [0, 5]");
+      if (variant < 0 || variant > 6) throw Error(ST_INVALID_ARGUMENT, "variant must be in [0, 6]");
       if (order < 0 || order > 2) throw Error(ST_INVALID_ARGUMENT, "order must be 0, 1 or 2");
       settings().warps.store(warps);
       settings().rowChunk.store(row_chunk);
@@ -211,6 +211,14 @@ extern "C"
       settings().bandBytes.store(band_bytes);
     });
   }
+
+  int sbg_set_window_cap(int cap)
+  {
+    if (cap < 0 || cap > (1 << 20)) { set_last_error("window cap must be in [0, 1048576]"); return SBG_ERR_INVALID_ARGUMENT; }
+    settings().windowCap.store(cap);
+    return SBG_OK;
+  }
+  int sbg_get_window_cap(void) { return settings().windowCap.load(); }
 
   int sbg_set_output_mode(int mode)
   {

@@ -219,9 +219,11 @@ namespace sbg
       pl.row_cap = 0;
       pl.smem_bytes = 0;
     }
-    else
+    else if (variant == 4 || (variant == 0 && sizeof(T) == 8))
     {
-      // hybrid: columns staged when the group fits, rows through L1
+      // hybrid: columns staged when the group fits, rows through L1 (the
+      // automatic choice for long double PCFs, where the FP64 pipe bounds
+      // both and the time-windowed walk measured slower)
       pl.smem = true;
       pl.packed = true;
       pl.kvar = 3;
@@ -230,6 +232,15 @@ namespace sbg
       pl.lmax_c = std::min(lmax_c, cap);
       pl.row_cap = 0;
       pl.smem_bytes = (size_t)32 * pl.lmax_c * es;
+    }
+    else
+    {
+      // time-windowed shared memory (float PCFs too long for the plain
+      // layout); the layout is sized below, once the rows per item are known
+      pl.smem = true;
+      pl.packed = false;
+      pl.kvar = 6;
+      pl.warps = want_w > 0 ? std::min(want_w, 32) : 24;
     }
 
     // Rows per item = 32 q: as large as possible (fewer column reloads,
@@ -246,10 +257,42 @@ namespace sbg
       }
     }
     pl.q = q;
+    if (pl.kvar == 6)
+    {
+      bool fit = false;
+      for (int w = pl.warps; w >= 4 && !fit; w -= 4)
+        fit = window_layout(pl, es, w, 32 * q, std::max(lmax_r, lmax_c), usable);
+      if (!fit) throw Error(ST_INVALID_ARGUMENT, "time-windowed variant: the window setting does not fit in shared memory");
+    }
     const uint64_t items = items_for(mode, 0, nr, nc, q);
     const int ctas_per_sm = (pl.kvar == 0) ? 2 : 1;
     pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(items, (uint64_t)dev.sms * ctas_per_sm));
     return pl;
+  }
+
+  bool window_layout(Plan& pl, size_t es, int warps, uint32_t rows_per_item, uint32_t lmax, size_t usable,
+                     uint32_t cap)
+  {
+    const uint32_t U = (uint32_t)kernel_unroll(es == 16);
+    const size_t slots = ((size_t)rows_per_item * 4 + 15) / 16 * 16;
+    auto bytes = [&](uint32_t X) { return (size_t)32 * X * es + (size_t)warps * (2 * X + U + 1) * es + slots; };
+    const uint32_t top = std::max<uint32_t>(8, (lmax + 7) / 8 * 8);
+    uint32_t X = cap ? cap : (uint32_t)std::max(0, settings().windowCap.load());
+    if (X == 0)
+    {
+      // bytes(X) is linear in X: the largest multiple of 8 that fits
+      const size_t fixed = bytes(0), per = bytes(1) - bytes(0);
+      if (usable < fixed + 8 * per) return false;
+      X = (uint32_t)std::min<size_t>((usable - fixed) / per / 8 * 8, top);
+    }
+    if (bytes(X) > usable) return false;
+    pl.warps = warps;
+    pl.lmax_c = X;
+    pl.win_r = X;
+    pl.row_cap = 2 * X + U + 1;
+    pl.row_slots = rows_per_item;
+    pl.smem_bytes = bytes(X);
+    return true;
   }
 
   template Plan make_plan<float>(int, uint64_t, uint64_t, const LengthStats&, const LengthStats&, const DeviceInfo&);
@@ -365,6 +408,8 @@ namespace sbg
     L.queue = queue;
     L.lmax_c = pl.lmax_c;
     L.row_cap = pl.row_cap;
+    L.win_r = pl.win_r;
+    L.row_slots = pl.row_slots;
     const int grid = (int)std::min<uint64_t>((uint64_t)pl.grid, d.n_items);
     SBG_CUDA(launch_pairs<T>(L, opk, pl.kvar, pl.warps, grid, pl.smem_bytes, st));
   }

@@ -424,6 +424,333 @@ namespace sbg
     }
   }
 
+  // ---- time-windowed variant: long PCFs in shared memory, window by window ----
+  //
+  // For PCFs too long for a 32-column block plus per-warp row buffers.  A
+  // work item walks consecutive time windows [A, B).  B is the earliest,
+  // over the item's 32 columns, end time of a column's lmax_c-th element
+  // counted from its first element ending after A, so no column slice holds
+  // more than lmax_c elements.  A row holding more than win_r elements in
+  // [A, B) is walked in pieces of at most win_r elements, each a sub-window
+  // [Ap, Bp) (Bp the end of the piece's last element) in which every lane
+  // starts its column at the first element ending after Ap.  Window ends
+  // thus depend on the column group alone, and a pair's rounding on neither
+  // the rows per item nor the warps per CTA.  Slices are staged like whole
+  // PCFs in the shared-memory variant, with the last element's end set to
+  // TMAX, and every rectangle is clipped to end at the (sub-)window end: the
+  // warp-uniform steps past a lane's end add zero-width rectangles only, and
+  // no side ever steps past its slice.  Integrals over [0, inf) split into
+  // the window integrals exactly (the rectangles meeting a window are those
+  // of the whole merge, cut at its ends).  Sums carry from piece to piece in
+  // registers and from window to window through the output element (raw
+  // sums, the finalizer after the last window), which the same CTA reads
+  // back after a block barrier.
+
+  __device__ __forceinline__ float earlier3(float a, float b, float c)
+  {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+  }
+  __device__ __forceinline__ double earlier3(double a, double b, double c) { return earlier(earlier(a, b), c); }
+
+  // Times >= 0 (and TMAX) order as their bit patterns read as unsigned
+  // integers, which shared-memory atomicMin handles for both widths.
+  template <typename T> struct TimeBits;
+  template <> struct TimeBits<float>
+  {
+    using U = unsigned int;
+    __device__ static __forceinline__ U of(float x) { return __float_as_uint(x); }
+    __device__ static __forceinline__ float val(U u) { return __uint_as_float(u); }
+    __device__ static __forceinline__ U warp_min(U x) { return __reduce_min_sync(0xffffffffu, x); }
+  };
+  template <> struct TimeBits<double>
+  {
+    using U = unsigned long long;
+    __device__ static __forceinline__ U of(double x) { return (U)__double_as_longlong(x); }
+    __device__ static __forceinline__ double val(U u) { return __longlong_as_double((long long)u); }
+    __device__ static __forceinline__ U warp_min(U x)
+    {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+      {
+        const U y = __shfl_xor_sync(0xffffffffu, x, o);
+        x = y < x ? y : x;
+      }
+      return x;
+    }
+  };
+
+  // Moves k0 past the elements of a PCF (CSR points pts, len elements) that
+  // end at or before A; the last element ends at TMAX > A.  Returns whether
+  // k0 moved.
+  template <typename T>
+  __device__ __forceinline__ bool slice_start(const T* pts, uint32_t len, uint32_t& k0, T A)
+  {
+    bool moved = false;
+    while (k0 + 1 < len && clamp_time(pts[2 * ((uint64_t)k0 + 1)]) <= A)
+    {
+      ++k0;
+      moved = true;
+    }
+    return moved;
+  }
+
+  // merge_smem_soa over one window: starts at t0 with the running sum acc0,
+  // clips every rectangle to end at tend, returns the raw compensated sum.
+  template <typename T, int K, int U>
+  __device__ __forceinline__ T merge_window(const T* ft0, uint32_t voff, const Elem<T>* pg, uint32_t steps, T t0,
+                                            T tend, T acc0, T p)
+  {
+    T fv = *reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(ft0) + voff);
+    T ft = *ft0;
+    Elem<T> G = *pg;
+    uint32_t af = (uint32_t)__cvta_generic_to_shared(ft0);
+    uint32_t ag = (uint32_t)__cvta_generic_to_shared(pg);
+    T t = t0, acc = acc0, comp = T(0);
+    const uint32_t nblk = (steps + U - 1) / U;
+    for (uint32_t b = 0; b < nblk; ++b)
+    {
+      T blk = T(0);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+      {
+        const T tn = earlier3(ft, G.tn, tend);
+        blk = accumulate<K>(blk, t, tn, fv, G.v, p);
+        t = tn;
+        advance_shared_soa(fv, ft, G.v, G.tn, af, voff, ag);
+      }
+      kahan_add(acc, comp, blk);
+    }
+    return acc - comp;
+  }
+
+  // Shared memory: the column block (lmax_c x 32 elements, interleaved), one
+  // row buffer per warp (row_cap elements' bytes: times, then values), and the
+  // saved slice start of each row of the item (row_slots words).
+  template <typename T, int K, int U>
+  __global__ void __launch_bounds__(1024, 1) pairs_window_kernel(const __grid_constant__ LaunchParams<T> L)
+  {
+    using TB = TimeBits<T>;
+    using UB = typename TB::U;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const uint32_t CW = L.lmax_c, RW = L.win_r;
+    Elem<T>* cols = reinterpret_cast<Elem<T>*>(smem_raw);
+    Elem<T>* rows = cols + (size_t)CW * 32;
+    uint32_t* rk0 = reinterpret_cast<uint32_t*>(rows + (size_t)nwarps * L.row_cap);
+    T* rt = reinterpret_cast<T*>(rows + (size_t)warp * L.row_cap);
+    T* rv = rt + L.row_cap;
+    const uint32_t voff = L.row_cap * (uint32_t)sizeof(T);
+    __shared__ unsigned long long s_item;
+    __shared__ unsigned int s_next_row;
+    __shared__ UB s_bend;
+    __shared__ uint32_t s_ck0[32], s_cnt[32], s_cm[32];
+    const T TM = tmax_of<T>();
+    const UB TMB = TB::of(TM);
+
+    for (;;)
+    {
+      if (threadIdx.x == 0) s_item = atomicAdd(L.queue, 1ull);
+      __syncthreads();
+      const unsigned long long item = s_item;
+      if (item >= L.total_items) break;
+
+      const ProblemDesc<T>* Pp = L.probs ? L.probs + find_problem(L.probs, L.n_probs, item) : &L.one;
+      const int mode = Pp->mode;
+      const uint64_t nc = Pp->nc;
+      const uint64_t G = ceil_div_u64(nc, 32);
+      const uint64_t local = item - Pp->item_begin;
+      uint64_t c, g;
+      if (mode == MODE_CROSS) { c = local / G; g = local % G; }
+      else tri_decode(local, Pp->row_begin, Pp->row_end, Pp->q, G, &c, &g);
+      uint64_t row_lo = Pp->row_begin + c * 32ull * Pp->q;
+      uint64_t row_hi = row_lo + 32ull * Pp->q;
+      if (row_hi > Pp->row_end) row_hi = Pp->row_end;
+      const uint64_t col0 = 32ull * g;
+      if (mode != MODE_CROSS)
+      {
+        const uint64_t first = col0 + (mode == MODE_PDIST ? 1 : 0);
+        if (row_lo < first) row_lo = first;
+      }
+      const uint32_t nrows = row_hi > row_lo ? (uint32_t)(row_hi - row_lo) : 0u;
+
+      // This lane's column (lanes past the last column mirror lane 0's).
+      const uint64_t cj = col0 + lane;
+      const bool cvalid = cj < nc;
+      const uint64_t cj_eff = cvalid ? cj : col0;
+      uint64_t corig = Pp->cperm ? Pp->cperm[cj_eff] : cj_eff;
+      const bool pgood = corig < nc;
+      if (!pgood) corig = 0;
+      const uint64_t coff = Pp->coff[corig];
+      const uint32_t clen = (uint32_t)(Pp->coff[corig + 1] - coff);
+      const T p = Pp->p;
+      const T* cp = Pp->cpts + 2 * coff;
+
+      // CTA-uniform: every warp holds the same 32 columns.
+      if (!__any_sync(FULL, clen == 0) && nrows > 0 && nrows <= L.row_slots)
+      {
+        for (uint32_t r = threadIdx.x; r < nrows; r += blockDim.x) rk0[r] = 0;
+        if (threadIdx.x < 32) s_ck0[threadIdx.x] = 0;
+        T A = T(0);
+        bool first = true;
+        for (;;)
+        {
+          if (threadIdx.x < 32) s_cnt[threadIdx.x] = 0;
+          if (threadIdx.x == 0) s_next_row = 0;
+
+          // Window end: the earliest, over the 32 columns, end of the CW-th
+          // element counted from the column's first element ending after A
+          // (the start moves past elements ending at A, zero-width ones).
+          if (warp == 0)
+          {
+            uint32_t k0 = s_ck0[lane];
+            if (slice_start(cp, clen, k0, A)) s_ck0[lane] = k0;
+            const uint32_t k = k0 + CW - 1;
+            UB bmin = TMB;
+            if (k + 1 < clen) bmin = TB::of(clamp_time(cp[2 * ((uint64_t)k + 1)]));
+            bmin = TB::warp_min(bmin);
+            if (lane == 0) s_bend = bmin;
+          }
+          __syncthreads();
+          T B = TB::val(s_bend);
+          if (!(B > A)) B = TM;  // times out of order: one last window ends the walk
+          const bool last = TB::of(B) == TMB;
+
+          // Column slices: up to CW elements from each column's start; the
+          // slice ends at the first element ending at or after B.
+          {
+            const uint32_t k0c = s_ck0[lane];
+            const uint32_t availc = min(CW, clen - k0c);
+            uint32_t cnt = 0;
+            for (uint32_t k = warp; k < availc; k += nwarps)
+            {
+              const uint32_t kk = k0c + k;
+              Elem<T> el;
+              el.v = cp[2 * (uint64_t)kk + 1];
+              el.tn = (kk + 1 < clen) ? clamp_time(cp[2 * ((uint64_t)kk + 1)]) : TM;
+              cols[(size_t)k * 32 + lane] = el;
+              cnt += el.tn < B ? 1u : 0u;
+            }
+            if (cnt) atomicAdd(&s_cnt[lane], cnt);
+          }
+          __syncthreads();
+          if (warp == 0)
+          {
+            const uint32_t k0c = s_ck0[lane];
+            const uint32_t availc = min(CW, clen - k0c);
+            const uint32_t m = min(s_cnt[lane] + 1u, availc);
+            Elem<T>& el = cols[(size_t)(m - 1) * 32 + lane];
+            uint32_t nxt = k0c + m - (el.tn > B ? 1u : 0u);  // first element ending after B
+            if (nxt > clen - 1) nxt = clen - 1;
+            el.tn = TM;
+            s_cm[lane] = m;
+            s_ck0[lane] = nxt;
+          }
+          __syncthreads();
+          const uint32_t maxmc = warp_max_u32(s_cm[lane]);
+
+          for (;;)
+          {
+            unsigned r = 0;
+            if (lane == 0) r = atomicAdd(&s_next_row, 1u);
+            r = __shfl_sync(FULL, r, 0);
+            if (r >= nrows) break;
+            const uint64_t i = row_lo + r;
+            const uint64_t iorig = Pp->rperm ? Pp->rperm[i] : i;
+            if (iorig >= Pp->nr) continue;  // skipped alike by the window-end pass
+            const uint64_t roff = Pp->roff[iorig];
+            const uint32_t rlen = (uint32_t)(Pp->roff[iorig + 1] - roff);
+            if (rlen == 0) continue;
+
+            const bool ok = cvalid && pgood && (mode == MODE_CROSS || (mode == MODE_PDIST ? cj < i : cj <= i));
+            if (!__any_sync(FULL, ok)) continue;  // alike in every window
+            uint64_t idx;
+            if (mode == MODE_CROSS) idx = iorig * Pp->ld + corig;
+            else idx = condensed_index(mode, iorig, corig);
+            const uint64_t rel = idx - Pp->out_base;  // wraps for idx < out_base
+            const bool store = ok && rel < Pp->out_count;
+            T acc = (!first && store) ? Pp->out[rel] : T(0);
+
+            // The row's elements meeting [A, B), at most RW at a time: a row
+            // denser than the item's columns takes several pieces, each a
+            // sub-window [Ap, Bp) for which every lane starts its column at
+            // the first element ending after Ap.  A piece is staged like the
+            // column slices, plus sentinel padding for the warp-uniform steps.
+            uint32_t k0 = rk0[r], z, m;
+            T Ap = A;
+            bool first_piece = true;
+            for (;;)
+            {
+              uint32_t avail, c2;
+              for (;;)
+              {
+                avail = min(RW, rlen - k0);
+                const T* rp = Pp->rpts + 2 * (roff + k0);
+                uint32_t zl = 0, cl = 0;
+                for (uint32_t k = lane; k < avail; k += 32)
+                {
+                  const T e = (k0 + k + 1 < rlen) ? clamp_time(rp[2 * ((uint64_t)k + 1)]) : TM;
+                  rv[k] = rp[2 * (uint64_t)k + 1];
+                  rt[k] = e;
+                  zl += e <= Ap ? 1u : 0u;
+                  cl += e < B ? 1u : 0u;
+                }
+                z = __reduce_add_sync(FULL, zl);   // elements ending by Ap (skipped)
+                c2 = __reduce_add_sync(FULL, cl);  // elements ending before B
+                if (z < avail) break;
+                k0 += avail;  // all of them end by Ap; the last element ends at TMAX
+                __syncwarp();
+              }
+              const bool full = c2 + 1 <= avail;  // the piece reaches B
+              m = full ? (c2 + 1 > z ? c2 + 1 - z : 1u) : avail - z;
+              __syncwarp();
+              const T Bp = full ? B : rt[avail - 1];
+              const T vlast = rv[z + m - 1];
+              __syncwarp();
+              const uint32_t pad_end = z + m + maxmc + U;  // <= RW + CW + U < row_cap
+              for (uint32_t k = z + m - 1 + lane; k < pad_end; k += 32)
+              {
+                rv[k] = vlast;
+                rt[k] = TM;
+              }
+              __syncwarp();
+              uint32_t g0 = 0;
+              if (!first_piece)
+              {
+                // first element of this lane's column slice ending after Ap
+                uint32_t lo = 0, hi = s_cm[lane] - 1;  // that slice's last element ends at TMAX
+                while (lo < hi)
+                {
+                  const uint32_t mid = (lo + hi) >> 1;
+                  if (cols[(size_t)mid * 32 + lane].tn > Ap) hi = mid; else lo = mid + 1;
+                }
+                g0 = lo;
+              }
+              acc = merge_window<T, K, U>(rt + z, voff, cols + (size_t)g0 * 32 + lane, m + maxmc - 1, Ap, Bp, acc, p);
+              __syncwarp();
+              if (full) break;
+              k0 += z + m;
+              Ap = Bp;
+              first_piece = false;
+            }
+            // the element reaching B starts the next window (skipped there if
+            // it ends at B)
+            if (lane == 0) rk0[r] = k0 + z + m - 1;
+            if (store) Pp->out[rel] = last ? PairOp<K>::fin(acc, p) : acc;
+          }
+          __syncthreads();
+          if (last) break;
+          A = B;
+          first = false;
+        }
+      }
+      __syncthreads();
+    }
+  }
+
   // ---- hybrid variant: columns in shared memory, rows through L1 -------------
   //
   // Rows are read from the packed segment layout in global memory (all lanes
@@ -657,10 +984,31 @@ namespace sbg
   }
 
   template <typename T>
+  static cudaError_t launch_window(int opk, dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                                   const LaunchParams<T>& L)
+  {
+    constexpr int U = Unroll<T>::value;
+    void (*fn)(const LaunchParams<T>) = nullptr;
+    switch (opk)
+    {
+      case OPK_L1: fn = pairs_window_kernel<T, OPK_L1, U>; break;
+      case OPK_L2DIST: fn = pairs_window_kernel<T, OPK_L2DIST, U>; break;
+      case OPK_LP: fn = pairs_window_kernel<T, OPK_LP, U>; break;
+      case OPK_INNER: fn = pairs_window_kernel<T, OPK_INNER, U>; break;
+      default: return cudaErrorInvalidValue;
+    }
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    fn<<<grid, block, smem, s>>>(L);
+    return launched();
+  }
+
+  template <typename T>
   cudaError_t launch_pairs(const LaunchParams<T>& L, int opk, int variant, int warps, int grid,
                            size_t smem_bytes, cudaStream_t s)
   {
     dim3 g((unsigned)grid), b((unsigned)(warps * 32));
+    if (variant == 6) return launch_window<T>(opk, g, b, smem_bytes, s, L);
     if (variant == 1) return launch_op<T, 1>(opk, g, b, smem_bytes, s, L);
     if (variant == 2) return launch_op<T, 2>(opk, g, b, smem_bytes, s, L);
     if (variant == 5) return launch_op<T, 5>(opk, g, b, smem_bytes, s, L);

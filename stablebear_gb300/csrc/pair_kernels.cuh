@@ -163,8 +163,11 @@ namespace sbg
     int n_probs;
     uint64_t total_items;
     unsigned long long* queue;   // zeroed before launch
-    uint32_t lmax_c;             // max column length (shared-memory layout)
+    uint32_t lmax_c;             // max column length (shared-memory layout); time-windowed
+                                 // variant: elements of a column slice
     uint32_t row_cap;            // per-warp row buffer capacity (elements)
+    uint32_t win_r;              // time-windowed variant: elements of a row slice
+    uint32_t row_slots;          // time-windowed variant: rows of an item with saved slice starts
   };
 
   // ---- item decoding ------------------------------------------------------

@@ -65,7 +65,8 @@ namespace sbg
     // Engine knobs (0 = automatic).
     std::atomic<int> warps{0};
     std::atomic<int> rowChunk{0};        // Q: rows per work item = 32 * Q
-    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory (8-byte row elements), 2 global-memory, 3 shared-memory pointer walk, 4 hybrid, 5 shared-memory with row times and values apart
+    std::atomic<int> variant{0};         // 0 auto, 1 shared-memory (8-byte row elements), 2 global-memory, 3 shared-memory pointer walk, 4 hybrid, 5 shared-memory with row times and values apart, 6 time-windowed shared memory
+    std::atomic<int> windowCap{0};       // time-windowed variant: elements per slice (0 = the most that fit)
     std::atomic<int> order{0};           // 0 auto, 1 caller order, 2 length-sorted
     std::atomic<uint64_t> bandBytes{0};  // output bytes per pipeline band (0 = auto)
     std::atomic<int> outputMode{0};      // host results: 0 auto (staged), 1 staged copy, 2 direct stores (coherent hosts)
@@ -126,13 +127,16 @@ namespace sbg
   {
     bool smem = true;
     int kvar = 2;      // kernel variant: 0 global memory, 1 shared two-load walk, 2 shared predicated walk,
-                       // 3 hybrid (columns in shared memory, rows through L1)
+                       // 3 hybrid (columns in shared memory, rows through L1), 5 shared with row times and
+                       // values apart, 6 time-windowed shared memory
     bool packed = false;  // the kernel reads the packed segment layout (variants 0 and 3)
     int warps = 16;
     int grid = 1;
     uint32_t q = 1;
     uint32_t lmax_c = 0;
     uint32_t row_cap = 0;
+    uint32_t win_r = 0;      // time-windowed variant: row slice cap (lmax_c is the column slice cap)
+    uint32_t row_slots = 0;  // time-windowed variant: rows per item with saved slice starts
     size_t smem_bytes = 0;
   };
 
@@ -158,6 +162,13 @@ namespace sbg
   cudaError_t launch_pack(const T* pts, const uint64_t* off, uint64_t n, Elem<T>* out, uint64_t cap, int sms,
                           cudaStream_t s);
   int kernel_unroll(bool f64);
+
+  // Shared-memory layout of the time-windowed variant for `warps` warps and
+  // items of up to rows_per_item rows: slice caps (`cap`, else the setting,
+  // else the largest multiple of 8 that fits, at most lmax rounded up to 8),
+  // row buffer, row slots and bytes.  False when it does not fit.
+  bool window_layout(Plan& pl, size_t elem_bytes, int warps, uint32_t rows_per_item, uint32_t lmax, size_t usable,
+                     uint32_t cap = 0);
 
   // Control block of one host-side run (progress, cancellation).
   struct RunControl

@@ -52,9 +52,20 @@ def set_min_block_side(n: int):
 def set_tuning(warps: int = 0, row_chunk: int = 0, variant: int = 0, order: int = 0, band_bytes: int = 0):
     """Engine knobs (0 = automatic): warps per CTA, rows per work item / 32,
     kernel variant (1 shared-memory, 2 global-memory, 3 shared-memory two-load
-    walk, 4 hybrid, 5 shared-memory with row times and values apart), PCF order (1 as given,
-    2 sorted by breakpoint count), output bytes per pipeline band."""
+    walk, 4 hybrid, 5 shared-memory with row times and values apart, 6
+    time-windowed shared memory), PCF order (1 as given, 2 sorted by
+    breakpoint count), output bytes per pipeline band."""
     nat.check(nat.lib().sbg_set_tuning(int(warps), int(row_chunk), int(variant), int(order), int(band_bytes)))
+
+
+def set_window_cap(cap: int = 0):
+    """Time-windowed variant: the most elements of one PCF inside a time
+    window (0 = the most that fit in shared memory)."""
+    nat.check(nat.lib().sbg_set_window_cap(int(cap)))
+
+
+def get_window_cap() -> int:
+    return int(nat.lib().sbg_get_window_cap())
 
 
 def build_type() -> str:

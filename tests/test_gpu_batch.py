@@ -80,20 +80,47 @@ def test_batch_graph_replay_and_autotune_are_stable():
     b.close()
 
 
-def test_batch_long_pcfs_fall_back_inside_the_launch():
-    """Groups too long for the shared-memory column block read their columns
-    from global memory within the same launch."""
+@pytest.mark.parametrize("variant", [0, 4])
+def test_batch_long_pcfs(variant):
+    """PCFs far longer than a shared-memory slice: the time-windowed kernel
+    (the default) walks them window by window; the hybrid kernel (variant 4)
+    reads column groups too long for its block from global memory."""
+    import stablebear_gb300 as sb
     from stablebear_gb300 import synthetic
     from stablebear_gb300.batch import PairwiseBatch
     from oracle import oracle as orc
     lens = np.array([20, 6000, 40, 3, 7000, 15] * 7)
     pts, off = synthetic.gaussian(len(lens), lens, np.float32, seed=2)
     small = synthetic.plain_l1(90, seed=3)
-    b = PairwiseBatch([(pts, off), small], op="l1", graph=False)
+    sb.set_tuning(variant=variant)
+    try:
+        b = PairwiseBatch([(pts, off), small], op="l1", graph=False)
+    finally:
+        sb.set_tuning()
     got = [o.cpu().numpy() for o in b.run()]
     truth = orc.evaluate(pts, off, truth=True)
     assert rel_err(got[0], truth) <= 1e-5
     assert rel_err(got[1], orc.evaluate(*small)) <= 1e-5
+    b.close()
+
+
+def test_batch_windowed_with_small_windows():
+    """Window caps of 5 elements in a batch of uneven problems (every pair
+    crosses many windows), against the double-double oracle: with windows
+    this small the float32 sum is close to a naive one (bound 3e-5)."""
+    import stablebear_gb300 as sb
+    from stablebear_gb300.batch import PairwiseBatch
+    from oracle import oracle as orc
+    probs = _problems(8, 9, nmax=120, lmax=200)
+    sb.set_window_cap(5)
+    try:
+        b = PairwiseBatch(probs, op="l1", graph=False)
+    finally:
+        sb.set_window_cap(0)
+    outs = [o.cpu().numpy() for o in b.run()]
+    for (pts, off), got in zip(probs, outs):
+        if len(off) > 2:
+            assert rel_err(got, orc.evaluate(pts, off, truth=True)) <= 3e-5
     b.close()
 
 

@@ -211,7 +211,7 @@ def test_variants_orders_and_bands_agree():
     np.testing.assert_array_equal(srt, base)
 
 
-def test_long_pcfs_use_global_memory_path():
+def test_long_pcfs():
     import stablebear_gb300 as sb
     from stablebear_gb300 import synthetic
     from oracle import oracle as orc

@@ -8,7 +8,7 @@ checks each result against sbg_pairwise_device, the allocating entry point,
 with the tolerance the other parity tests use (float32: 1e-5 relative; here
 the two paths run the same kernel, so the results are in fact identical).
 It also checks the clear rejection of a problem too large for the fixed
-scratch.  This file is collected last so a failure here cannot hide others.
+scratch (the hybrid kernel's packed copy of long PCFs).  This file is collected last so a failure here cannot hide others.
 """
 import ctypes
 
@@ -69,14 +69,20 @@ def test_no_alloc_matches_allocating_entry(env):
     _run_pair(torch, nat, pts, off, nat.SKIP_LOWER, nat.OP_L2_INNER, 1.0)
 
 
-def test_no_alloc_long_pcfs_use_scratch_copy(env):
-    """PCFs too long for the shared-memory kernel: the packed copy of the
-    breakpoints goes into the fixed scratch."""
+@pytest.mark.parametrize("variant", [0, 4])
+def test_no_alloc_long_pcfs(env, variant):
+    """PCFs too long for the plain shared-memory layout: the time-windowed
+    kernel (the default) reads the breakpoints in place; the hybrid kernel
+    (variant 4) puts its packed copy into the fixed scratch."""
     torch, nat = env
     from stablebear_gb300 import synthetic
     lens = np.array([3, 9000, 5, 1, 7000, 12] * 5)
     pts, off = synthetic.gaussian(len(lens), lens, np.float32, seed=5)
-    _run_pair(torch, nat, pts, off, nat.SKIP_LOWER_NODIAG, nat.OP_LP, 2.0)
+    nat.check(nat.lib().sbg_set_tuning(0, 0, variant, 0, 0))
+    try:
+        _run_pair(torch, nat, pts, off, nat.SKIP_LOWER_NODIAG, nat.OP_LP, 2.0)
+    finally:
+        nat.check(nat.lib().sbg_set_tuning(0, 0, 0, 0, 0))
 
 
 def test_no_alloc_rejects_oversized_problem(env):
@@ -87,12 +93,26 @@ def test_no_alloc_rejects_oversized_problem(env):
     dp, do = _device_csr(torch, pts, off)
     out = torch.empty(190, dtype=torch.float32, device="cuda")
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    rc = nat.lib().sbg_pairwise_device_noalloc(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
-                                               do.data_ptr(), 20, int(off[-1]), None, None, 0, 0, None, None,
-                                               40_000, out.data_ptr(), 0, 0, 0, st)
+    # the hybrid kernel needs a packed copy of the breakpoints in the scratch
+    nat.check(nat.lib().sbg_set_tuning(0, 0, 4, 0, 0))
+    try:
+        rc = nat.lib().sbg_pairwise_device_noalloc(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                                   do.data_ptr(), 20, int(off[-1]), None, None, 0, 0, None, None,
+                                                   40_000, out.data_ptr(), 0, 0, 0, st)
+        msg = nat.last_error()
+    finally:
+        nat.check(nat.lib().sbg_set_tuning(0, 0, 0, 0, 0))
     assert rc == -1
-    msg = nat.last_error()
     assert "scratch" in msg and "limit" in msg
+    # the time-windowed kernel (the default) reads the breakpoints in place
+    ref = torch.empty(190, dtype=torch.float32, device="cuda")
+    nat.check(nat.lib().sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                            do.data_ptr(), 20, None, None, 0, None, None, 40_000, ref.data_ptr(),
+                                            0, 0, 0, st))
+    nat.check(nat.lib().sbg_pairwise_device_noalloc(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
+                                                    do.data_ptr(), 20, int(off[-1]), None, None, 0, 0, None, None,
+                                                    40_000, out.data_ptr(), 0, 0, 0, st))
+    assert torch.equal(out, ref)
     assert nat.lib().sbg_pairwise_device_noalloc(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),
                                                  do.data_ptr(), 20, int(off[-1]), None, None, 0, 0, None, None, 0,
                                                  out.data_ptr(), 0, 0, 0, st) == -1
