@@ -48,6 +48,8 @@ def parse():
                     help="processing order of the device entry: 0 length order (default), 1 caller order")
     ap.add_argument("--variant", type=int, default=0, choices=range(0, 7),
                     help="kernel variant of the engine (0 automatic; 4 hybrid, 5 shared memory, 6 time-windowed)")
+    ap.add_argument("--window-cap", type=int, default=0,
+                    help="time-windowed kernel: elements of a PCF per window (0 automatic)")
     ap.add_argument("--config", default="large",
                     choices=["large", "plain", "stable_rank", "batched", "fwdbwd", "dense"],
                     help="large: the headline workload; the others print their own report line")
@@ -113,6 +115,9 @@ def run_aux(args):
     if args.variant:
         nat.check(lib.sbg_set_tuning(0, 0, args.variant, 0, 0))
         rep["variant"] = args.variant
+    if args.window_cap:
+        nat.check(lib.sbg_set_window_cap(args.window_cap))
+        rep["window_cap"] = args.window_cap
 
     def single(pts, off, opc, p, skip, out, lmax):
         dp, do = _device_problem(pts, off)
@@ -290,6 +295,7 @@ def config(args, n, ws):
             "l2": "inputs (CSR) and output larger than L2; no flush",
             "processing_order": "caller" if getattr(args, "order", 0) == 1 else "length order in 1024-PCF windows",
             "generator_sha256": _generator_hash(),
+            "kernel_variant": getattr(args, "variant", 0) or "automatic",
             "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"}
 
 
@@ -439,6 +445,8 @@ def main():
 
     if args.order or args.variant:
         sb.set_tuning(order=args.order, variant=args.variant)
+    if args.window_cap:
+        sb.set_window_cap(args.window_cap)
 
     def step():
         nat.check(lib.sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(),

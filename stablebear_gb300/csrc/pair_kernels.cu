@@ -525,6 +525,21 @@ namespace sbg
     return acc - comp;
   }
 
+  // First k in [lo, hi] whose element of this lane's staged column ends
+  // after x (STRICT) or at or after x; element hi (a slice's last, ending at
+  // TMAX, or one already known to qualify) always does.
+  template <typename T, bool STRICT>
+  __device__ __forceinline__ uint32_t column_search(const Elem<T>* cols, int lane, uint32_t lo, uint32_t hi, T x)
+  {
+    while (lo < hi)
+    {
+      const uint32_t mid = (lo + hi) >> 1;
+      const T tn = cols[(size_t)mid * 32 + lane].tn;
+      if (STRICT ? tn > x : tn >= x) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+  }
+
   // Shared memory: the column block (lmax_c x 32 elements, interleaved), one
   // row buffer per warp (row_cap elements' bytes: times, then values), and the
   // saved slice start of each row of the item (row_slots words).
@@ -717,19 +732,15 @@ namespace sbg
                 rt[k] = TM;
               }
               __syncwarp();
-              uint32_t g0 = 0;
-              if (!first_piece)
-              {
-                // first element of this lane's column slice ending after Ap
-                uint32_t lo = 0, hi = s_cm[lane] - 1;  // that slice's last element ends at TMAX
-                while (lo < hi)
-                {
-                  const uint32_t mid = (lo + hi) >> 1;
-                  if (cols[(size_t)mid * 32 + lane].tn > Ap) hi = mid; else lo = mid + 1;
-                }
-                g0 = lo;
-              }
-              acc = merge_window<T, K, U>(rt + z, voff, cols + (size_t)g0 * 32 + lane, m + maxmc - 1, Ap, Bp, acc, p);
+              // This lane's column elements meeting [Ap, Bp): from the first
+              // ending after Ap to the first ending at or after Bp; the warp
+              // steps through the most of them (the whole slices for a piece
+              // that is the row's whole window).
+              uint32_t g0 = 0, g1 = s_cm[lane] - 1;
+              if (!first_piece) g0 = column_search<T, true>(cols, lane, 0, g1, Ap);
+              if (!full) g1 = column_search<T, false>(cols, lane, g0, g1, Bp);
+              const uint32_t ncol = (first_piece && full) ? maxmc : warp_max_u32(g1 - g0 + 1);
+              acc = merge_window<T, K, U>(rt + z, voff, cols + (size_t)g0 * 32 + lane, m + ncol - 1, Ap, Bp, acc, p);
               __syncwarp();
               if (full) break;
               k0 += z + m;
