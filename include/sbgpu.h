@@ -97,7 +97,9 @@ int sbg_get_device_verbose(void);
  * shared memory: each work item walks time windows holding at most a cap of
  * elements of every PCF, the automatic choice for longer PCFs), order
  * (1 caller's, 2 sorted
- * by breakpoint count), output bytes per pipeline band. */
+ * by breakpoint count), output bytes per pipeline band (automatic: 1/8 of
+ * the output, the last eighth cut into halving parts so that little of the
+ * copy-out runs after the last kernel). */
 int sbg_set_tuning(int warps, int row_chunk, int variant, int order, uint64_t band_bytes);
 
 /* Time-windowed variant: the most elements of one PCF inside a window

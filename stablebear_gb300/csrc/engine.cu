@@ -710,6 +710,7 @@ namespace sbg
     // with its later PCF in the band lands in the band's contiguous range
     // of the condensed (or dense) output.
     uint64_t band_bytes = settings().bandBytes.load();
+    const bool auto_bands = band_bytes == 0;
     if (band_bytes == 0) band_bytes = out_bytes > (512ull << 20) ? out_bytes / 8 + 1 : out_bytes;
     band_bytes = std::min<uint64_t>(band_bytes, budget / 2 > 0 ? budget / 2 : band_bytes);
     std::vector<std::pair<uint64_t, uint64_t>> bands;
@@ -740,6 +741,24 @@ namespace sbg
         }
         bands.emplace_back(rb, re);
         rb = re;
+      }
+      // Nothing overlaps the last band's copy-out: with automatic sizes it
+      // is cut into parts of 1/2, 1/4, ... of its row units (one unit each
+      // at the end), so the exposed copy is about one unit's output.
+      if (auto_bands && bands.size() > 1)
+      {
+        const auto last = bands.back();
+        bands.pop_back();
+        uint64_t b0 = last.first;
+        uint64_t units = (last.second - b0 + align - 1) / align;
+        while (units > 1)
+        {
+          const uint64_t take = units / 2;
+          bands.emplace_back(b0, b0 + take * align);
+          b0 += take * align;
+          units -= take;
+        }
+        bands.emplace_back(b0, last.second);
       }
     }
     uint64_t max_band = 0;
