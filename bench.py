@@ -51,8 +51,10 @@ def parse():
     ap.add_argument("--window-cap", type=int, default=0,
                     help="time-windowed kernel: elements of a PCF per window (0 automatic)")
     ap.add_argument("--config", default="large",
-                    choices=["large", "plain", "stable_rank", "batched", "fwdbwd", "dense"],
-                    help="large: the headline workload; the others print their own report line")
+                    choices=["large", "plain", "stable_rank", "batched", "fwdbwd", "dense", "ref_gpu_kernel"],
+                    help="large: the headline workload; the others print their own report line; "
+                         "ref_gpu_kernel (with --impl reference): the reference's own CUDA block kernel "
+                         "on the headline workload's shape at --n PCFs")
     return ap.parse_args()
 
 
@@ -377,8 +379,52 @@ class ClockSampler:
 
 # ---- reference arm ---------------------------------------------------------------
 
+def run_reference_gpu_kernel(args):
+    """The reference's own CUDA block kernel (a cubin of its headers, driven
+    tile by tile with its scheduler's parameters) on the headline workload's
+    PCFs at N = --n: the tile kernels' device time, CSR resident."""
+    import torch
+    from oracle import oracle as orc
+    from stablebear_gb300 import synthetic
+    ok = orc.ref_gpu_kernel_available()
+    if ok is not True:
+        print(json.dumps({"impl": "reference", "config_name": "ref_gpu_kernel", "unavailable": ok}), flush=True)
+        return
+    n = args.n
+    pts, off = workload(n, seed=0)
+    pairs = n * (n - 1) // 2
+    segs = synthetic.segment_count(off, pts, 1)
+    dp = torch.from_numpy(pts).cuda()
+    do = torch.from_numpy(off.astype(np.int64)).cuda()
+    torch.cuda.synchronize()
+    steps = args.steps if n <= 30_000 else 1
+    runs = [orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), n) for _ in range(steps)]
+    ms = min(r[0] for r in runs)
+    tiles = runs[0][1]
+    line = {"impl": "reference", "config_name": "ref_gpu_kernel", "metric": METRIC, "value": pairs / (ms / 1e3),
+            "unit": UNIT, "n_gpus": 1, "steps": steps, "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic", "config": config(args, n, 1),
+            "segments_per_s": segs / (ms / 1e3), "tiles": tiles,
+            "kernel": "sb::internal::cuda_pcf_block_integrate<float, float, OperationL1Dist> compiled from the "
+                      "reference's headers for sm_103a; block 1x32; tiles of the reference scheduler "
+                      "(32 splits, min side sqrt(SMs*1024), 80% of free memory)",
+            "timed": "the tile kernels only (CSR resident on the device; no tile clearing, copies or host scatter)"}
+    if n <= 30_000:
+        hout = np.full(pairs, np.nan, np.float32)
+        orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), n, host_out=hout)
+        rows = np.unique(np.linspace(1, n - 1, 24).astype(np.uint64))
+        want, starts = orc.evaluate_rows(pts, off, rows)
+        got = np.concatenate([hout[int(i) * (int(i) - 1) // 2: int(i) * (int(i) - 1) // 2 + int(i)] for i in rows])
+        line["max_rel_err_vs_reference_cpu"] = float(np.max(np.abs(got.astype(np.float64) - want) /
+                                                            np.maximum(np.abs(want), 1e-30)))
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
+        return
+    if args.config == "ref_gpu_kernel":
+        run_reference_gpu_kernel(args)
         return
     pts, off = workload(args.n, seed=0)
     threads = os.cpu_count() or 1
@@ -413,6 +459,8 @@ def main():
     if args.impl == "reference":
         run_reference(args, ws, rank)
         return
+    if args.config == "ref_gpu_kernel":
+        raise SystemExit("--config ref_gpu_kernel times the reference's kernel: use it with --impl reference")
     if args.config != "large":
         if rank == 0:
             run_aux(args)

@@ -7,6 +7,15 @@
   stablebear reference's own headers.  Built only when the reference tree is
   present (``SBREF_ROOT``, default ``/root/reference``); the reference is
   never copied into this repository.
+* ``oracle/_ref/ref_kernels.cubin`` + ``ref_kernels.json`` — the reference's
+  own CUDA block kernel (``ref_gpu_kernel.cu`` instantiating
+  ``include/sbear/cuda/cuda_pcf_kernel.cuh``), device code only, for sm_103a,
+  with its entry names as ptxas prints them.  Built only where the reference
+  tree is present; a cubin carries no host code, so it also loads on hosts of
+  another CPU architecture.
+* ``oracle/_ref/libsbrefgpu.so`` — ``ref_gpu.cpp``, the host harness that
+  loads that cubin through the CUDA driver API; built wherever the CUDA
+  toolkit is (it holds no reference code).
 """
 from __future__ import annotations
 
@@ -50,7 +59,63 @@ def build_ref(force: bool = False) -> str | None:
     return REF_SO
 
 
+REF_CUBIN = os.path.join(REF_DIR, "ref_kernels.cubin")
+REF_ENTRIES = os.path.join(REF_DIR, "ref_kernels.json")
+REF_GPU_SO = os.path.join(REF_DIR, "libsbrefgpu.so")
+
+
+def _cuda_home() -> str:
+    for cand in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if cand and os.path.isdir(os.path.join(cand, "include")):
+            return cand
+    raise RuntimeError("CUDA toolkit not found")
+
+
+def build_ref_gpu_kernel(force: bool = False) -> str | None:
+    """The reference's block kernel as a cubin, plus its entry names."""
+    import json
+    import re
+    inc = os.path.join(REF_ROOT, "include")
+    if not os.path.isdir(os.path.join(inc, "sbear")):
+        return None
+    src = os.path.join(HERE, "ref_gpu_kernel.cu")
+    os.makedirs(REF_DIR, exist_ok=True)
+    if force or _stale(REF_CUBIN, [src, __file__]) or not os.path.exists(REF_ENTRIES):
+        nvcc = os.path.join(_cuda_home(), "bin", "nvcc")
+        # the reference's CUDA options (CMakeLists.txt: --expt-relaxed-constexpr,
+        # BUILD_WITH_CUDA=1, release optimisation); whole-program device code
+        cmd = [nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+               "--expt-relaxed-constexpr", "-DBUILD_WITH_CUDA=1", "-Xptxas", "-v", "-I", inc,
+               "-o", REF_CUBIN, src]
+        r = subprocess.run(cmd, capture_output=True, text=True, check=True)
+        names = re.findall(r"Compiling entry function '([^']+)'", r.stdout + r.stderr)
+        entries = {}
+        for nm in names:
+            for key, tag in (("l1", "OperationL1Dist"), ("lp", "OperationLpDist"), ("inner", "OperationL2InnerProduct")):
+                if tag in nm:
+                    entries[key] = nm
+        with open(REF_ENTRIES, "w") as f:
+            json.dump(entries, f, indent=1)
+    return REF_CUBIN
+
+
+def build_ref_gpu_harness(force: bool = False) -> str:
+    src = os.path.join(HERE, "ref_gpu.cpp")
+    os.makedirs(REF_DIR, exist_ok=True)
+    hdr = os.path.join(HERE, "..", "include", "sbgpu", "compat.hpp")
+    if force or _stale(REF_GPU_SO, [src, hdr, __file__]):
+        cuda = _cuda_home()
+        libdirs = [d for d in (os.path.join(cuda, "lib64"), os.path.join(cuda, "lib64", "stubs"),
+                               os.path.join(cuda, "targets", "sbsa-linux", "lib", "stubs")) if os.path.isdir(d)]
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", os.path.join(cuda, "include"),
+               "-o", REF_GPU_SO, src] + [f"-L{d}" for d in libdirs] + ["-lcuda"]
+        subprocess.run(cmd, check=True)
+    return REF_GPU_SO
+
+
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref(force))
+    print(build_ref_gpu_kernel(force))
+    print(build_ref_gpu_harness(force))

@@ -327,3 +327,65 @@ def barcodes_to_pcfs(bars, bar_offsets, kind):
     rc = lib.sbo_barcodes_to_pcfs(kind, _dtype_code(bars), _ptr(bars), _ptr(boff), n, _ptr(out), _ptr(ooff))
     assert rc == 0
     return out[: int(ooff[-1])], ooff
+
+
+_ref_gpu = None
+
+
+def ref_gpu_kernel_available():
+    """Whether the reference's own CUDA block kernel (a cubin built where the
+    reference tree is) and its driver-API harness are present; a reason
+    string otherwise."""
+    import json
+    if not os.path.exists(_build.REF_CUBIN) or not os.path.exists(_build.REF_ENTRIES):
+        return "no oracle/_ref/ref_kernels.cubin (it is built where the reference tree is present)"
+    try:
+        _build.build_ref_gpu_harness()
+    except Exception as e:  # pragma: no cover
+        return f"harness not built: {e}"
+    with open(_build.REF_ENTRIES) as f:
+        if not json.load(f):
+            return "no kernel entries recorded"
+    return True
+
+
+def ref_gpu_triangle(dev_points_ptr, dev_offsets_ptr, n, *, op="l1", p=1.0, kernel=False, host_out=None,
+                     max_output_elements=0):
+    """Run the reference's own CUDA block kernel over the pdist (or, with
+    kernel=True, the L2-kernel) triangle of n float32 PCFs whose CSR is on
+    the current CUDA device (points (t, v) pairs and uint64 offsets, given as
+    device addresses), tile by tile with the reference scheduler's
+    parameters.  Returns (summed tile-kernel milliseconds, tiles).  With
+    host_out (a float32 array of the condensed size) the tiles are also
+    scattered into it."""
+    import json
+    global _ref_gpu
+    ok = ref_gpu_kernel_available()
+    if ok is not True:
+        raise RuntimeError(ok)
+    if _ref_gpu is None:
+        lib = ctypes.CDLL(_build.build_ref_gpu_harness())
+        lib.sbref_gpu_triangle.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_float, _U64, _U64,
+                                           _U64, _P, _U64, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_uint64), ctypes.c_char_p, ctypes.c_size_t]
+        lib.sbref_gpu_triangle.restype = ctypes.c_int
+        _ref_gpu = lib
+    with open(_build.REF_ENTRIES) as f:
+        entries = json.load(f)
+    key = "inner" if kernel else op
+    if key not in entries:
+        raise ValueError(f"no reference kernel for {key}")
+    ms = ctypes.c_double(0.0)
+    tiles = ctypes.c_uint64(0)
+    err = ctypes.create_string_buffer(512)
+    hp = None
+    if host_out is not None:
+        assert host_out.dtype == np.float32 and host_out.flags["C_CONTIGUOUS"]
+        assert host_out.size == out_size(MODE_KERNEL if kernel else MODE_PDIST, n)
+        hp = _ptr(host_out)
+    rc = _ref_gpu.sbref_gpu_triangle(_build.REF_CUBIN.encode(), entries[key].encode(), 2 if kernel else 1, float(p),
+                                     int(dev_points_ptr), int(dev_offsets_ptr), int(n), hp, int(max_output_elements),
+                                     ctypes.byref(ms), ctypes.byref(tiles), err, len(err))
+    if rc != 0:
+        raise RuntimeError(err.value.decode())
+    return ms.value, int(tiles.value)
