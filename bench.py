@@ -401,9 +401,12 @@ def run_reference_gpu_kernel(args):
     runs = [orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), n) for _ in range(steps)]
     ms = min(r[0] for r in runs)
     tiles = runs[0][1]
+    cfg = config(args, n, 1)
+    cfg["processing_order"] = "caller order, tiles of the reference scheduler"
+    cfg["kernel_variant"] = "the reference's block kernel"
     line = {"impl": "reference", "config_name": "ref_gpu_kernel", "metric": METRIC, "value": pairs / (ms / 1e3),
             "unit": UNIT, "n_gpus": 1, "steps": steps, "ms_per_step": ms, "higher_is_better": True,
-            "dtype": "f32", "data": "synthetic", "config": config(args, n, 1),
+            "dtype": "f32", "data": "synthetic", "config": cfg,
             "segments_per_s": segs / (ms / 1e3), "tiles": tiles,
             "kernel": "sb::internal::cuda_pcf_block_integrate<float, float, OperationL1Dist> compiled from the "
                       "reference's headers for sm_103a; block 1x32; tiles of the reference scheduler "
@@ -438,10 +441,13 @@ def run_reference(args, ws, rank):
         times.append(dt)
         pairs_tot += pairs
     value = pairs_tot / sum(times)
+    cfg = config(args, args.n, ws)
+    cfg["processing_order"] = "caller order (sampled rows, all host threads)"
+    cfg["kernel_variant"] = "the reference's CPU algorithm"
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config(args, args.n, ws),
+            "config": cfg,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{len(rows)} rows of the N={args.n} triangle "
                                        f"({pairs_tot // max(1, args.steps)} pairs per step), "
