@@ -423,11 +423,83 @@ def run_reference_gpu_kernel(args):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_aux(args):
+    """The reference's own CUDA block kernel on the other workloads (the
+    reference has no batched launch: one tiled run per problem; no
+    gradients, no device dense expansion)."""
+    import torch
+    from oracle import oracle as orc
+    from stablebear_gb300 import synthetic
+    rep = {"impl": "reference", "config_name": args.config, "data": "synthetic",
+           "kernel": "the reference's sb::internal::cuda_pcf_block_integrate (cubin of its headers), tiles of its "
+                     "scheduler, block 1x32; tile kernels only, CSR resident"}
+    ok = orc.ref_gpu_kernel_available()
+    if ok is not True or args.config in ("fwdbwd", "dense"):
+        rep["unavailable"] = ok if ok is not True else (
+            "the reference has no gradients" if args.config == "fwdbwd" else
+            "the reference expands matrices on the host (py_distance_matrix.hpp:37-49), not on the device")
+        print(json.dumps(rep), flush=True)
+        return
+
+    def dev(pts, off):
+        return torch.from_numpy(pts).cuda(), torch.from_numpy(off.astype(np.int64)).cuda()
+
+    def sample_err(pts, off, n, dt, kw, oracle_kw, rows):
+        hout = np.full(n * (n + 1) // 2 if kw.get("kernel") else n * (n - 1) // 2, np.nan, dt)
+        dp, do = dev(pts, off)
+        orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), n, host_out=hout, dtype=dt, **kw)
+        want, starts = orc.evaluate_rows(pts, off, rows, **oracle_kw)
+        per = 1 if kw.get("kernel") else 0
+        got = np.concatenate([hout[(int(i) * (int(i) + 1) // 2 if per else int(i) * (int(i) - 1) // 2):][: int(i) + per]
+                              for i in rows]).astype(np.float64)
+        floor = 1.0 if per else 1e-300
+        return float(np.max(np.abs(got - want) / np.maximum(np.abs(want), floor)))
+
+    if args.config == "plain":
+        pts, off = synthetic.plain_l1(1000, seed=0)
+        dp, do = dev(pts, off)
+        ms = min(orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), 1000)[0] for _ in range(max(3, args.steps)))
+        rep.update({"workload": "L1 pdist N=1000 f32, L~U{10..200}", "gpu_ms": ms,
+                    "gpu_pairs_per_s": 499500 / (ms / 1e3),
+                    "max_rel_err_vs_reference_cpu": sample_err(pts, off, 1000, np.float32, {}, {},
+                                                               np.arange(1, 1000, 37, dtype=np.uint64))})
+    elif args.config == "stable_rank":
+        n = args.n if args.n != 100_000 else 20_000
+        pts, off = synthetic.stable_rank(n, seed=0)
+        dp, do = dev(pts, off)
+        rows = np.unique(np.random.default_rng(1).integers(1, n, size=24)).astype(np.uint64)
+        for name, kw, okw in (("l2_kernel", {"kernel": True}, {"op": orc.OP_L2, "mode": orc.MODE_KERNEL}),
+                              ("l2_pdist", {"op": "lp", "p": 2.0}, {"op": orc.OP_LP, "p": 2.0})):
+            ms, tiles = orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), n, dtype=np.float64, **kw)
+            cnt = n * (n + 1) // 2 if kw.get("kernel") else n * (n - 1) // 2
+            rep[name] = {"gpu_ms": ms, "tiles": tiles, "pairs": cnt, "gpu_pairs_per_s": cnt / (ms / 1e3),
+                         "max_rel_err_vs_reference_cpu": sample_err(pts, off, n, np.float64, kw, okw, rows[:6])}
+        rep["workload"] = f"N={n} f64 stable-rank-like, L=round(exp(U[ln16,ln4096]))"
+    elif args.config == "batched":
+        probs = synthetic.batched_betti(512, seed=0)
+        pairs = sum((len(o) - 1) * (len(o) - 2) // 2 for _, o in probs)
+        devs = [dev(p_, o) for p_, o in probs]
+        for name, kw in (("l1", {}), ("l2", {"op": "lp", "p": 2.0})):
+            ms = 0.0
+            for (p_, o), (dp, do) in zip(probs, devs):
+                ms += orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), len(o) - 1, **kw)[0]
+            rep[name] = {"gpu_ms": ms, "gpu_pairs_per_s": pairs / (ms / 1e3)}
+        p0, o0 = probs[0]
+        rep["max_rel_err_vs_reference_cpu"] = sample_err(p0, o0, len(o0) - 1, np.float32, {}, {},
+                                                         np.arange(1, len(o0) - 1, 41, dtype=np.uint64))
+        rep.update({"workload": "512 problems, N_i~U{50..2000}, L~U{8..1024}, f32 Betti-like; one tiled "
+                                "reference run per problem", "pairs": pairs})
+    print(json.dumps(rep), flush=True)
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
     if args.config == "ref_gpu_kernel":
         run_reference_gpu_kernel(args)
+        return
+    if args.config != "large":
+        run_reference_aux(args)
         return
     pts, off = workload(args.n, seed=0)
     threads = os.cpu_count() or 1

@@ -91,9 +91,13 @@ def build_ref_gpu_kernel(force: bool = False) -> str | None:
         names = re.findall(r"Compiling entry function '([^']+)'", r.stdout + r.stderr)
         entries = {}
         for nm in names:
+            # the template arguments <float, float, ...> / <double, double, ...> mangle as "Iff" / "Idd"
+            suffix = "_f32" if "integrateIff" in nm else ("_f64" if "integrateIdd" in nm else None)
+            if suffix is None:
+                continue
             for key, tag in (("l1", "OperationL1Dist"), ("lp", "OperationLpDist"), ("inner", "OperationL2InnerProduct")):
                 if tag in nm:
-                    entries[key] = nm
+                    entries[key + suffix] = nm
         with open(REF_ENTRIES, "w") as f:
             json.dump(entries, f, indent=1)
     return REF_CUBIN

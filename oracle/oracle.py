@@ -350,14 +350,14 @@ def ref_gpu_kernel_available():
 
 
 def ref_gpu_triangle(dev_points_ptr, dev_offsets_ptr, n, *, op="l1", p=1.0, kernel=False, host_out=None,
-                     max_output_elements=0):
+                     max_output_elements=0, dtype=np.float32):
     """Run the reference's own CUDA block kernel over the pdist (or, with
-    kernel=True, the L2-kernel) triangle of n float32 PCFs whose CSR is on
-    the current CUDA device (points (t, v) pairs and uint64 offsets, given as
-    device addresses), tile by tile with the reference scheduler's
-    parameters.  Returns (summed tile-kernel milliseconds, tiles).  With
-    host_out (a float32 array of the condensed size) the tiles are also
-    scattered into it."""
+    kernel=True, the L2-kernel) triangle of n PCFs of `dtype` (float32 or
+    float64) whose CSR is on the current CUDA device (points (t, v) pairs and
+    uint64 offsets, given as device addresses), tile by tile with the
+    reference scheduler's parameters.  Returns (summed tile-kernel
+    milliseconds, tiles).  With host_out (an array of `dtype` and the
+    condensed size) the tiles are also scattered into it."""
     import json
     global _ref_gpu
     ok = ref_gpu_kernel_available()
@@ -365,14 +365,18 @@ def ref_gpu_triangle(dev_points_ptr, dev_offsets_ptr, n, *, op="l1", p=1.0, kern
         raise RuntimeError(ok)
     if _ref_gpu is None:
         lib = ctypes.CDLL(_build.build_ref_gpu_harness())
-        lib.sbref_gpu_triangle.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_float, _U64, _U64,
-                                           _U64, _P, _U64, ctypes.POINTER(ctypes.c_double),
-                                           ctypes.POINTER(ctypes.c_uint64), ctypes.c_char_p, ctypes.c_size_t]
+        lib.sbref_gpu_triangle.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_double, _U64, _U64, _U64, _P, _U64,
+                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
+                                           ctypes.c_char_p, ctypes.c_size_t]
         lib.sbref_gpu_triangle.restype = ctypes.c_int
         _ref_gpu = lib
     with open(_build.REF_ENTRIES) as f:
         entries = json.load(f)
-    key = "inner" if kernel else op
+    dtype = np.dtype(dtype)
+    if dtype not in (np.float32, np.float64):
+        raise TypeError("float32 or float64 PCFs")
+    key = ("inner" if kernel else op) + ("_f32" if dtype == np.float32 else "_f64")
     if key not in entries:
         raise ValueError(f"no reference kernel for {key}")
     ms = ctypes.c_double(0.0)
@@ -380,10 +384,11 @@ def ref_gpu_triangle(dev_points_ptr, dev_offsets_ptr, n, *, op="l1", p=1.0, kern
     err = ctypes.create_string_buffer(512)
     hp = None
     if host_out is not None:
-        assert host_out.dtype == np.float32 and host_out.flags["C_CONTIGUOUS"]
+        assert host_out.dtype == dtype and host_out.flags["C_CONTIGUOUS"]
         assert host_out.size == out_size(MODE_KERNEL if kernel else MODE_PDIST, n)
         hp = _ptr(host_out)
-    rc = _ref_gpu.sbref_gpu_triangle(_build.REF_CUBIN.encode(), entries[key].encode(), 2 if kernel else 1, float(p),
+    rc = _ref_gpu.sbref_gpu_triangle(_build.REF_CUBIN.encode(), entries[key].encode(), dtype.itemsize,
+                                     2 if kernel else 1, float(p),
                                      int(dev_points_ptr), int(dev_offsets_ptr), int(n), hp, int(max_output_elements),
                                      ctypes.byref(ms), ctypes.byref(tiles), err, len(err))
     if rc != 0:

@@ -20,8 +20,9 @@
 // copied back and scattered into condensed storage (parity checks).
 //
 // The kernel is reached through the CUDA driver API (cuModuleLoad,
-// cuLaunchKernel) with the parameter block of PcfBlockKernelParams<float,
-// float> (cuda_pcf_kernel.cuh:19-31) restated below; every launch is checked.
+// cuLaunchKernel) with the parameter block of PcfBlockKernelParams<T, T>
+// (cuda_pcf_kernel.cuh:19-31, T = float or double) restated below; every
+// launch is checked.
 #include <cuda.h>
 
 #include <algorithm>
@@ -37,13 +38,13 @@
 
 namespace
 {
-  // PcfBlockKernelParams<float, float>: pointers, sizes, TriangleSkipMode (int).
+  // PcfBlockKernelParams<T, T>: pointers, sizes, TriangleSkipMode (int).
   struct RefParams
   {
-    float* matrix;
+    void* matrix;
     uint64_t* rowTimePointOffsets;
     uint64_t* colTimePointOffsets;
-    const void* rowPoints;  // SimplePoint<float, float> {t, v}: the CSR's interleaved layout
+    const void* rowPoints;  // SimplePoint<T, T> {t, v}: the CSR's interleaved layout
     const void* colPoints;
     uint64_t nRows, nCols, globalRowStart, globalColStart;
     int skipMode;
@@ -66,14 +67,17 @@ namespace
   }
 }
 
-extern "C" int sbref_gpu_triangle(const char* cubin, const char* entry, int skip_mode, float p, uint64_t dpts,
-                                  uint64_t doff, uint64_t n, float* host_out, uint64_t max_output_elements,
-                                  double* kernel_ms, uint64_t* n_tiles, char* err, size_t errlen)
+namespace
+{
+  template <typename T>
+  int run_triangle(const char* cubin, const char* entry, int skip_mode, double p, uint64_t dpts, uint64_t doff,
+                   uint64_t n, T* host_out, uint64_t max_output_elements, double* kernel_ms, uint64_t* n_tiles,
+                   char* err, size_t errlen)
 {
   CUmodule mod = nullptr;
   CUdeviceptr tile = 0;
   CUevent e0 = nullptr, e1 = nullptr;
-  std::vector<float> htile;
+  std::vector<T> htile;
   try
   {
     if (skip_mode != 1 && skip_mode != 2) throw Fail{"skip_mode must be 1 (pdist) or 2 (kernel)"};
@@ -93,7 +97,7 @@ extern "C" int sbref_gpu_triangle(const char* cubin, const char* entry, int skip
     {
       size_t freeb = 0, totalb = 0;
       check(cuMemGetInfo(&freeb, &totalb), "cuMemGetInfo");
-      max_output_elements = (uint64_t)((double)freeb * 0.8) / 2 / sizeof(float) / 1024 * 1024;
+      max_output_elements = (uint64_t)((double)freeb * 0.8) / 2 / sizeof(T) / 1024 * 1024;
     }
     const uint64_t min_side = (uint64_t)std::sqrt((double)sms * 1024.0);
     sb::CudaBlockScheduler sched({(size_t)n, (size_t)n, (size_t)max_output_elements, 32,
@@ -102,21 +106,21 @@ extern "C" int sbref_gpu_triangle(const char* cubin, const char* entry, int skip
     if (n_tiles) *n_tiles = blocks.size();
     const size_t cap = sched.max_row_height() * sched.max_col_width();
     if (cap == 0) { if (kernel_ms) *kernel_ms = 0; cuModuleUnload(mod); return 0; }
-    check(cuMemAlloc(&tile, cap * sizeof(float)), "tile buffer");
+    check(cuMemAlloc(&tile, cap * sizeof(T)), "tile buffer");
     if (host_out) htile.resize(cap);
     check(cuEventCreate(&e0, CU_EVENT_DEFAULT), "event");
     check(cuEventCreate(&e1, CU_EVENT_DEFAULT), "event");
 
     const unsigned bx = 1, by = 32;  // the reference's default block (settings blockDimX, blockDimY)
-    const float a = 0.f, b = FLT_MAX;
+    const T a = T(0), b = sizeof(T) == 4 ? T(FLT_MAX) : T(DBL_MAX);  // numeric_limits<T>::max()
     const unsigned char op_l1 = 0;  // empty operation objects (L1 distance, L2 inner product)
-    const float op_lp = p;          // OperationLpDist holds p
+    const T op_lp = T(p);           // OperationLpDist holds p
     const bool lp = std::strstr(entry, "OperationLpDist") != nullptr;
     double total_ms = 0.0;
     for (const auto& blk : blocks)
     {
       RefParams prm;
-      prm.matrix = reinterpret_cast<float*>(tile);
+      prm.matrix = reinterpret_cast<void*>(tile);
       prm.rowTimePointOffsets = reinterpret_cast<uint64_t*>(doff) + blk.rowStart;
       prm.colTimePointOffsets = reinterpret_cast<uint64_t*>(doff) + blk.colStart;
       prm.rowPoints = reinterpret_cast<const void*>(dpts);
@@ -128,7 +132,7 @@ extern "C" int sbref_gpu_triangle(const char* cubin, const char* entry, int skip
       prm.skipMode = skip_mode;
       const unsigned gx = (unsigned)((blk.rowHeight + bx - 1) / bx);
       const unsigned gy = (unsigned)((blk.colWidth + by - 1) / by);
-      void* args[] = {&prm, const_cast<float*>(&a), const_cast<float*>(&b),
+      void* args[] = {&prm, const_cast<T*>(&a), const_cast<T*>(&b),
                       lp ? (void*)&op_lp : (void*)&op_l1};
       check(cuEventRecord(e0, nullptr), "event record");
       check(cuLaunchKernel(fn, gx, gy, 1, bx, by, 1, 0, nullptr, args, nullptr), "cuLaunchKernel");
@@ -139,7 +143,7 @@ extern "C" int sbref_gpu_triangle(const char* cubin, const char* entry, int skip
       total_ms += ms;
       if (host_out)
       {
-        check(cuMemcpyDtoH(htile.data(), tile, blk.rowHeight * blk.colWidth * sizeof(float)), "tile copy");
+        check(cuMemcpyDtoH(htile.data(), tile, blk.rowHeight * blk.colWidth * sizeof(T)), "tile copy");
         for (size_t il = 0; il < blk.rowHeight; ++il)
         {
           const uint64_t i = blk.rowStart + il;
@@ -169,4 +173,21 @@ extern "C" int sbref_gpu_triangle(const char* cubin, const char* entry, int skip
     if (mod) cuModuleUnload(mod);
     return -1;
   }
+}
+}
+
+// elem_bytes 4: float CSR and output, 8: double.
+extern "C" int sbref_gpu_triangle(const char* cubin, const char* entry, int elem_bytes, int skip_mode, double p,
+                                  uint64_t dpts, uint64_t doff, uint64_t n, void* host_out,
+                                  uint64_t max_output_elements, double* kernel_ms, uint64_t* n_tiles, char* err,
+                                  size_t errlen)
+{
+  if (elem_bytes == 4)
+    return run_triangle<float>(cubin, entry, skip_mode, p, dpts, doff, n, static_cast<float*>(host_out),
+                               max_output_elements, kernel_ms, n_tiles, err, errlen);
+  if (elem_bytes == 8)
+    return run_triangle<double>(cubin, entry, skip_mode, p, dpts, doff, n, static_cast<double*>(host_out),
+                                max_output_elements, kernel_ms, n_tiles, err, errlen);
+  if (err && errlen) std::snprintf(err, errlen, "elem_bytes must be 4 or 8");
+  return -1;
 }

@@ -17,3 +17,9 @@ template __global__ void sb::internal::cuda_pcf_block_integrate<float, float, sb
     sb::internal::PcfBlockKernelParams<float, float>, float, float, sb::OperationLpDist<float, float>);
 template __global__ void sb::internal::cuda_pcf_block_integrate<float, float, sb::OperationL2InnerProduct<float, float>>(
     sb::internal::PcfBlockKernelParams<float, float>, float, float, sb::OperationL2InnerProduct<float, float>);
+template __global__ void sb::internal::cuda_pcf_block_integrate<double, double, sb::OperationL1Dist<double, double>>(
+    sb::internal::PcfBlockKernelParams<double, double>, double, double, sb::OperationL1Dist<double, double>);
+template __global__ void sb::internal::cuda_pcf_block_integrate<double, double, sb::OperationLpDist<double, double>>(
+    sb::internal::PcfBlockKernelParams<double, double>, double, double, sb::OperationLpDist<double, double>);
+template __global__ void sb::internal::cuda_pcf_block_integrate<double, double, sb::OperationL2InnerProduct<double, double>>(
+    sb::internal::PcfBlockKernelParams<double, double>, double, double, sb::OperationL2InnerProduct<double, double>);

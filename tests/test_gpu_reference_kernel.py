@@ -71,3 +71,22 @@ def test_reference_kernel_l2_kernel(env):
     ours = sb.l2_kernel(sb.PcfArray.from_csr(pts, off)).data
     truth = orc.evaluate(pts, off, op=orc.OP_L2, mode=orc.MODE_KERNEL, truth=True)
     assert rel(ours, truth, floor=1.0) <= 1e-5
+
+
+def test_reference_kernel_f64(env):
+    """Double precision (the stable-rank workload's type): the reference's own
+    GPU-vs-CPU tolerance for double is 1e-10 (test/test_block_integrate.cu:43)."""
+    import torch
+    import stablebear_gb300 as sb
+    from stablebear_gb300 import synthetic
+    orc = env[0]
+    pts, off = synthetic.stable_rank(400, seed=3)
+    n = len(off) - 1
+    dp = torch.from_numpy(pts).cuda()
+    do = torch.from_numpy(off.astype(np.int64)).cuda()
+    out = np.full(n * (n + 1) // 2, np.nan, np.float64)
+    orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), n, kernel=True, host_out=out, dtype=np.float64)
+    want = orc.evaluate(pts, off, op=orc.OP_L2, mode=orc.MODE_KERNEL)
+    assert rel(out, want, floor=1.0) <= 1e-10
+    ours = sb.l2_kernel(sb.PcfArray.from_csr(pts, off)).data
+    assert rel(ours, want, floor=1.0) <= 1e-12
