@@ -106,7 +106,8 @@ namespace sbg
       L.row_cap = pl.row_cap;
       L.win_r = pl.win_r;
       L.row_slots = pl.row_slots;
-      const int grid = (int)std::min<uint64_t>((uint64_t)dev.sms, total_items);
+      const int grid = (int)std::min<uint64_t>((uint64_t)dev.sms * ctas_per_sm(dev, pl.warps, pl.smem_bytes),
+                                                 total_items);
       SBG_CUDA(launch_pairs<T>(L, opk, pl.kvar, pl.warps, grid, pl.smem_bytes, st));
     }
 

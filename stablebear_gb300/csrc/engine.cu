@@ -96,8 +96,23 @@ namespace sbg
     int optin = 0;
     SBG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     d.smem_optin = (size_t)optin;
+    int per_sm = 0, threads = 0;
+    SBG_CUDA(cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    SBG_CUDA(cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+    d.smem_per_sm = (size_t)per_sm;
+    d.threads_per_sm = threads;
     cache[dev] = d;
     return d;
+  }
+
+  int ctas_per_sm(const DeviceInfo& dev, int warps, size_t smem_bytes)
+  {
+    const int threads = std::max(1, warps) * 32;
+    int n = std::max(1, dev.threads_per_sm / threads);
+    n = std::min(n, std::max(1, 65536 / (threads * 64)));  // the register file at 64 per thread
+    const size_t per = smem_bytes + 1024;
+    if (smem_bytes > 0 && dev.smem_per_sm > 0) n = std::min<int>(n, std::max<size_t>(1, dev.smem_per_sm / per));
+    return n;
   }
 
   // ---- input contract ------------------------------------------------------
@@ -257,6 +272,16 @@ namespace sbg
       }
     }
     pl.q = q;
+    // Problems too small for 6 items per SM even at 32 rows per item: two
+    // CTAs of 16 warps per SM, so one CTA's column staging and row fills
+    // overlap the other's merges (N = 1000: 123.5 against 141 us).
+    if (settings().warps.load() == 0 && settings().rowChunk.load() == 0 && pl.kvar == 5 && q == 1 &&
+        pl.warps > 16 && items_for(mode, 0, nr, nc, 1) < (uint64_t)dev.sms * 6 &&
+        ctas_per_sm(dev, 16, smem_for(16)) >= 2)
+    {
+      pl.warps = 16;
+      pl.smem_bytes = smem_for(16);
+    }
     if (pl.kvar == 6)
     {
       bool fit = false;
@@ -265,8 +290,8 @@ namespace sbg
       if (!fit) throw Error(ST_INVALID_ARGUMENT, "time-windowed variant: the window setting does not fit in shared memory");
     }
     const uint64_t items = items_for(mode, 0, nr, nc, q);
-    const int ctas_per_sm = (pl.kvar == 0) ? 2 : 1;
-    pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(items, (uint64_t)dev.sms * ctas_per_sm));
+    const int per_sm = (pl.kvar == 0) ? 2 : ctas_per_sm(dev, pl.warps, pl.smem_bytes);
+    pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(items, (uint64_t)dev.sms * per_sm));
     return pl;
   }
 

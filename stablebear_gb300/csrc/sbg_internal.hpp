@@ -103,9 +103,16 @@ namespace sbg
   {
     int device = 0;
     int sms = 0;
-    size_t smem_optin = 0;
+    size_t smem_optin = 0;   // shared memory one CTA may opt in to
+    size_t smem_per_sm = 0;  // shared memory of one SM (all its CTAs)
+    int threads_per_sm = 0;
   };
   DeviceInfo device_info();
+
+  // Resident CTAs per SM of a persistent pair kernel (64 registers per
+  // thread, launch_bounds(1024, 1)) with `warps` warps and `smem_bytes` of
+  // dynamic shared memory (plus 1 KB the runtime reserves per CTA).
+  int ctas_per_sm(const DeviceInfo& dev, int warps, size_t smem_bytes);
 
   // A set of PCFs in the reference's CSR layout.
   template <typename T>

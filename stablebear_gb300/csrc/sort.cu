@@ -9,10 +9,10 @@
 // global sort scatters every store and multiplied DRAM traffic ~9x).  The
 // order is computed on the stream, with no host round trip.
 //
-// Keys (window << 42 | min(length, 2^32 - 1) << 10 | index in window) are
-// unique, so a bitonic network (not stable by itself) gives the one
-// deterministic order.  Each window is sorted by one CTA in shared memory;
-// the last window is padded with all-ones keys, which sort last.
+// Keys (min(length, 2^32 - 1) << 10 | index in window) are unique within a
+// window, so a bitonic network (not stable by itself) gives the one
+// deterministic order.  Each window is keyed, sorted and written out by one
+// CTA in shared memory, in one launch.
 #include "../../include/sbgpu.h"
 #include "sbg_internal.hpp"
 
@@ -22,8 +22,7 @@ namespace sbg
 {
   namespace
   {
-    constexpr int SORT_THREADS = 1024;
-    constexpr uint64_t SORT_TILE = 2 * SORT_THREADS;
+    constexpr int SORT_THREADS = LENGTH_ORDER_WINDOW / 2;  // one compare-exchange per thread and stage
 
     __device__ __forceinline__ void cmp_swap(uint64_t& a, uint64_t& b, bool ascending)
     {
@@ -35,88 +34,59 @@ namespace sbg
       }
     }
 
-    // Stages k = k_first .. k_last (powers of two) with partner distances
-    // j = min(k / 2, j_first) .. 1, on one tile in shared memory.  Every tile
-    // is sorted on its own, ascending: the direction of a comparison comes
-    // from the index inside the tile.
-    __global__ void __launch_bounds__(SORT_THREADS) tile_stages_kernel(uint64_t* keys, uint64_t n, uint64_t tile,
-                                                                       uint64_t k_first, uint64_t k_last,
-                                                                       uint64_t j_first)
+    // One CTA per window: keys (min(length, 2^32 - 1) << 10 | index in
+    // window) built from the offsets, a bitonic network in shared memory,
+    // the permutation written out.  A stage whose partner distance j is at
+    // most 32 pairs elements inside the 64 that one warp handles, so it only
+    // needs the warp's own barrier after a stage of the same kind; a block
+    // barrier precedes every stage that crosses warps and the stage after it.
+    // The last window is padded with all-ones keys, which sort last.
+    __global__ void __launch_bounds__(SORT_THREADS) window_order_kernel(const uint64_t* __restrict__ off, uint64_t n,
+                                                                        uint32_t* __restrict__ perm)
     {
-      __shared__ uint64_t s[SORT_TILE];
-      const uint64_t base = (uint64_t)blockIdx.x * tile;
-      for (uint64_t i = threadIdx.x; i < tile; i += blockDim.x) s[i] = keys[base + i];
-      __syncthreads();
-      for (uint64_t k = k_first; k <= k_last; k <<= 1)
+      __shared__ uint64_t s[LENGTH_ORDER_WINDOW];
+      const uint64_t base = (uint64_t)blockIdx.x * LENGTH_ORDER_WINDOW;
+      for (uint32_t i = threadIdx.x; i < LENGTH_ORDER_WINDOW; i += SORT_THREADS)
       {
-        for (uint64_t j = (k / 2 < j_first ? k / 2 : j_first); j > 0; j >>= 1)
+        const uint64_t g = base + i;
+        uint64_t key = ~0ull;
+        if (g < n)
         {
-          for (uint64_t t = threadIdx.x; t < tile / 2; t += blockDim.x)
-          {
-            const uint64_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));  // j is a power of two
-            cmp_swap(s[i], s[i + j], (i & k) == 0);
-          }
-          __syncthreads();
-        }
-      }
-      for (uint64_t i = threadIdx.x; i < tile; i += blockDim.x) keys[base + i] = s[i];
-      (void)n;
-    }
-
-    __global__ void make_keys_kernel(const uint64_t* __restrict__ off, uint64_t n, uint64_t npad,
-                                     uint64_t* __restrict__ keys)
-    {
-      for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += (uint64_t)gridDim.x * blockDim.x)
-      {
-        if (i < n)
-        {
-          uint64_t len = off[i + 1] - off[i];
+          uint64_t len = off[g + 1] - off[g];
           if (len > 0xffffffffull) len = 0xffffffffull;
-          keys[i] = ((i >> 10) << 42) | (len << 10) | (i & 1023);
+          key = (len << 10) | i;
         }
-        else keys[i] = ~0ull;
+        s[i] = key;
       }
-    }
-
-    __global__ void keys_to_perm_kernel(const uint64_t* __restrict__ keys, uint64_t n, uint32_t* __restrict__ perm)
-    {
-      for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        perm[i] = (uint32_t)(((keys[i] >> 42) << 10) | (keys[i] & 1023));
+      uint32_t prev_j = LENGTH_ORDER_WINDOW;  // the loads cross warps
+      for (uint32_t k = 2; k <= LENGTH_ORDER_WINDOW; k <<= 1)
+      {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1)
+        {
+          if (j >= 64 || prev_j >= 64) __syncthreads(); else __syncwarp();
+          const uint32_t t = threadIdx.x;
+          const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1));  // j is a power of two
+          cmp_swap(s[i], s[i + j], (i & k) == 0);
+          prev_j = j;
+        }
+      }
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < LENGTH_ORDER_WINDOW; i += SORT_THREADS)
+        if (base + i < n) perm[base + i] = (uint32_t)(base + (s[i] & 1023));
     }
   }
 
   static_assert(LENGTH_ORDER_WINDOW == 1024, "the key layout holds 10 bits of index within a window");
-  static_assert(LENGTH_ORDER_WINDOW <= SORT_TILE, "a window is sorted inside one tile");
 
-  // Keys padded to whole windows (or, below one window, to a power of two).
-  static uint64_t padded_keys(uint64_t n)
-  {
-    if (n >= LENGTH_ORDER_WINDOW) return (n + LENGTH_ORDER_WINDOW - 1) / LENGTH_ORDER_WINDOW * LENGTH_ORDER_WINDOW;
-    uint64_t npad = 1;
-    while (npad < n) npad <<= 1;
-    return npad;
-  }
+  // The order needs no global scratch; kept for callers that size one.
+  uint64_t length_order_scratch_bytes(uint64_t) { return 0; }
 
-  uint64_t length_order_scratch_bytes(uint64_t n) { return padded_keys(n) * sizeof(uint64_t); }
-
-  void length_order_device(const uint64_t* off, uint64_t n, uint32_t* perm, void* scratch, cudaStream_t st)
+  void length_order_device(const uint64_t* off, uint64_t n, uint32_t* perm, void*, cudaStream_t st)
   {
     if (n == 0) return;
     if (n > 0xffffffffull) throw Error(ST_INVALID_ARGUMENT, "too many PCFs for a 32-bit processing order");
-    const uint64_t npad = padded_keys(n);
-    uint64_t* keys = static_cast<uint64_t*>(scratch);
-    const unsigned blocks = (unsigned)std::min<uint64_t>((npad + 255) / 256, 4096);
-    make_keys_kernel<<<blocks, 256, 0, st>>>(off, n, npad, keys);
-    SBG_CUDA(launched());
-    // The window sits in the keys' high bits, so sorting every window on its
-    // own (one tile each) is the whole sort.
-    const uint64_t tile = npad < LENGTH_ORDER_WINDOW ? npad : LENGTH_ORDER_WINDOW;
-    if (tile >= 2)
-    {
-      tile_stages_kernel<<<(unsigned)(npad / tile), SORT_THREADS, 0, st>>>(keys, npad, tile, 2, tile, tile / 2);
-      SBG_CUDA(launched());
-    }
-    keys_to_perm_kernel<<<blocks, 256, 0, st>>>(keys, n, perm);
+    const uint64_t windows = (n + LENGTH_ORDER_WINDOW - 1) / LENGTH_ORDER_WINDOW;
+    window_order_kernel<<<(unsigned)windows, SORT_THREADS, 0, st>>>(off, n, perm);
     SBG_CUDA(launched());
   }
 }
@@ -128,13 +98,7 @@ extern "C" int sbg_length_order_device(const uint64_t* offsets, uint64_t n, uint
   {
     if (n && (!offsets || !perm)) throw Error(ST_INVALID_ARGUMENT, "null pointer");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    void* keys = nullptr;
-    if (n)
-    {
-      SBG_CUDA(cudaMallocAsync(&keys, length_order_scratch_bytes(n), st));
-      struct Free { void* p; cudaStream_t s; ~Free() { cudaFreeAsync(p, s); } } guard{keys, st};
-      length_order_device(offsets, n, perm, keys, st);
-    }
+    if (n) length_order_device(offsets, n, perm, nullptr, st);
     set_last_error("");
     return ST_OK;
   }
