@@ -28,6 +28,9 @@ namespace sbg
   {
     constexpr int TILE = 32;
     constexpr int ROWS = 8;  // thread rows per CTA: 32 x 8 threads, 4 rows each
+#ifndef D2C_TILE
+#define D2C_TILE 64
+#endif
 
     __device__ __forceinline__ uint64_t cond_index(bool diag, uint64_t i, uint64_t j)
     {
@@ -167,28 +170,31 @@ namespace sbg
 
     // Flags (bit set = violated somewhere): 1 not symmetric, 2 non-zero
     // diagonal (distance matrices), 4 negative entry (distance matrices).
-    template <typename T>
-    __global__ void __launch_bounds__(TILE * ROWS) dense_to_condensed_kernel(
+    // TD x TD tiles (TD = 64: each row piece of a tile, and of its mirror,
+    // is 256 contiguous bytes read by two warps, against 128 with 32-wide
+    // tiles; the reads of the two triangles dominate this kernel's traffic).
+    template <typename T, int TD>
+    __global__ void __launch_bounds__(TD * ROWS) dense_to_condensed_kernel(
         const T* __restrict__ dense, uint64_t n, uint64_t ld, bool diag, T* __restrict__ cond,
         unsigned int* __restrict__ flags, TileSet ts)
     {
-      __shared__ T upper[TILE][TILE + 1];
+      __shared__ T upper[TD][TD + 1];
       const int tx = threadIdx.x, ty = threadIdx.y;
       unsigned int f = 0;
       for (uint64_t k = blockIdx.x; k < ts.count; k += gridDim.x)
       {
         uint64_t a, b;
         ts.decode(k, &a, &b);
-        const uint64_t i0 = a * TILE, j0 = b * TILE;
-        if (a > b && i0 + TILE <= n)
+        const uint64_t i0 = a * TD, j0 = b * TD;
+        if (a > b && i0 + TD <= n)
         {
           // interior tile: no bound checks, row-pointer walks, and the
           // condensed row starts advance by i (+1 with the diagonal)
           const T* up = dense + (j0 + ty) * ld + i0 + tx;
           const T* lo = dense + (i0 + ty) * ld + j0 + tx;
-          T low[TILE / ROWS];
+          T low[TD / ROWS];
 #pragma unroll
-          for (int q = 0; q < TILE / ROWS; ++q)
+          for (int q = 0; q < TD / ROWS; ++q)
           {
             upper[tx][ty + q * ROWS] = up[0];
             low[q] = lo[0];
@@ -199,7 +205,7 @@ namespace sbg
           uint64_t i = i0 + ty;
           T* dst = cond + cond_index(diag, i, 0) + j0 + tx;
 #pragma unroll
-          for (int q = 0; q < TILE / ROWS; ++q)
+          for (int q = 0; q < TD / ROWS; ++q)
           {
             const T v = low[q];
             if (!(v == upper[ty + q * ROWS][tx])) f |= 1u;
@@ -213,9 +219,9 @@ namespace sbg
         }
         // The mirror tile (b, a), read coalesced and kept transposed, and
         // this thread's values of the lower tile, all loads before the barrier.
-        T low[TILE / ROWS];
+        T low[TD / ROWS];
 #pragma unroll
-        for (int q = 0; q < TILE / ROWS; ++q)
+        for (int q = 0; q < TD / ROWS; ++q)
         {
           const int r = ty + q * ROWS;
           const uint64_t i = j0 + r, j = i0 + tx;
@@ -225,7 +231,7 @@ namespace sbg
         }
         __syncthreads();
 #pragma unroll
-        for (int q = 0; q < TILE / ROWS; ++q)
+        for (int q = 0; q < TD / ROWS; ++q)
         {
           const int r = ty + q * ROWS;
           const uint64_t i = i0 + r, j = j0 + tx;
@@ -331,19 +337,22 @@ extern "C"
       if (ld < n) throw Error(ST_INVALID_ARGUMENT, "ld must be >= n");
       if (!dense || (!condensed && output_count(skip, n, n) > 0))
         throw Error(ST_INVALID_ARGUMENT, "null matrix pointer");
-      const uint64_t nb = ceil_div_u64(n, TILE);
+      constexpr int TD = D2C_TILE;
+      const uint64_t nb = ceil_div_u64(n, TD);
       TileSet ts;
       ts.init(0, nb, nb);
       cudaStream_t st = (cudaStream_t)stream;
-      const dim3 block(TILE, ROWS);
-      const int grid = grid_for(ts.count);
+      const dim3 block(TD, ROWS);
+      // 8 x 256 threads per SM at TD = 32; the same threads in 4 x 512 at 64
+      const int grid = (int)std::min<uint64_t>(std::max<uint64_t>(ts.count, 1),
+                                               (uint64_t)device_info().sms * (2048 / (TD * ROWS)));
       const bool diag = skip == SBG_SKIP_LOWER;
       if (dtype == SBG_F32)
-        dense_to_condensed_kernel<float><<<grid, block, 0, st>>>((const float*)dense, n, ld, diag, (float*)condensed,
-                                                                  flags, ts);
+        dense_to_condensed_kernel<float, TD><<<grid, block, 0, st>>>((const float*)dense, n, ld, diag,
+                                                                      (float*)condensed, flags, ts);
       else
-        dense_to_condensed_kernel<double><<<grid, block, 0, st>>>((const double*)dense, n, ld, diag,
-                                                                   (double*)condensed, flags, ts);
+        dense_to_condensed_kernel<double, TD><<<grid, block, 0, st>>>((const double*)dense, n, ld, diag,
+                                                                       (double*)condensed, flags, ts);
       SBG_CUDA(launched());
     });
   }
