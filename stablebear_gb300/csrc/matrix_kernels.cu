@@ -26,10 +26,15 @@ namespace sbg
 {
   namespace
   {
-    constexpr int TILE = 32;
-    constexpr int ROWS = 8;  // thread rows per CTA: 32 x 8 threads, 4 rows each
+    constexpr int ROWS = 8;  // thread rows per CTA: TD x 8 threads, TD / 8 rows of a TD-wide tile each
 #ifndef D2C_TILE
 #define D2C_TILE 64
+#endif
+// condensed -> dense keeps two 32-wide tiles per iteration: its writes
+// merge in L2, and one 64-wide tile measured slower (12.2 against 11.7 ms
+// at N = 100,000)
+#ifndef C2D_TILE
+#define C2D_TILE 32
 #endif
 
     __device__ __forceinline__ uint64_t cond_index(bool diag, uint64_t i, uint64_t j)
@@ -76,34 +81,36 @@ namespace sbg
       }
     };
 
-    // Two tiles per CTA iteration, both loaded before the barrier, so each
-    // thread keeps eight loads in flight.
-    template <typename T>
-    __global__ void __launch_bounds__(TILE * ROWS) condensed_to_dense_kernel(
+    // NT tiles of TD x TD per CTA iteration, all loaded before the barrier,
+    // so each thread keeps NT * TD / ROWS loads in flight (eight for both
+    // shapes used: two 32-wide tiles, or one 64-wide tile whose row pieces,
+    // read and written, are 256 contiguous bytes instead of 128).
+    template <typename T, int TD, int NT>
+    __global__ void __launch_bounds__(TD * ROWS) condensed_to_dense_kernel(
         const T* __restrict__ cond, uint64_t n, bool diag, T* __restrict__ dense, uint64_t ld,
         uint64_t row_begin, uint64_t row_end, TileSet ts)
     {
-      __shared__ T tile[2][TILE][TILE + 1];
+      __shared__ T tile[NT][TD][TD + 1];
       const int tx = threadIdx.x, ty = threadIdx.y;
-      for (uint64_t k0 = 2ull * blockIdx.x; k0 < ts.count; k0 += 2ull * gridDim.x)
+      for (uint64_t k0 = (uint64_t)NT * blockIdx.x; k0 < ts.count; k0 += (uint64_t)NT * gridDim.x)
       {
-        uint64_t a[2], b[2];
-        const int nt = k0 + 1 < ts.count ? 2 : 1;
-        T v[2][TILE / ROWS];
+        uint64_t a[NT], b[NT];
+        const int nt = k0 + NT <= ts.count ? NT : (int)(ts.count - k0);
+        T v[NT][TD / ROWS];
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
+        for (int u = 0; u < NT; ++u)
         {
           if (u < nt) ts.decode(k0 + u, &a[u], &b[u]);
           else { a[u] = 0; b[u] = 0; }
-          const uint64_t i0 = a[u] * TILE, j = b[u] * TILE + tx;
-          if (u < nt && a[u] > b[u] && i0 + TILE <= n)
+          const uint64_t i0 = a[u] * TD, j = b[u] * TD + tx;
+          if (u < nt && a[u] > b[u] && i0 + TD <= n)
           {
             // interior tile: every element exists, no per-element checks;
             // consecutive rows' starts differ by i (+1 with the diagonal)
             uint64_t i = i0 + ty;
             const T* src = cond + cond_index(diag, i, 0) + j;
 #pragma unroll
-            for (int q = 0; q < TILE / ROWS; ++q)
+            for (int q = 0; q < TD / ROWS; ++q)
             {
               v[u][q] = src[0];
               // start of row i + ROWS minus start of row i
@@ -114,7 +121,7 @@ namespace sbg
           else
           {
 #pragma unroll
-            for (int q = 0; q < TILE / ROWS; ++q)
+            for (int q = 0; q < TD / ROWS; ++q)
             {
               const uint64_t i = i0 + ty + q * ROWS;
               v[u][q] = (u < nt && i < n && j < n && (j < i || (diag && j == i))) ? cond[cond_index(diag, i, j)] : T(0);
@@ -122,21 +129,21 @@ namespace sbg
           }
         }
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
+        for (int u = 0; u < NT; ++u)
 #pragma unroll
-          for (int q = 0; q < TILE / ROWS; ++q) tile[u][ty + q * ROWS][tx] = v[u][q];
+          for (int q = 0; q < TD / ROWS; ++q) tile[u][ty + q * ROWS][tx] = v[u][q];
         __syncthreads();
         for (int u = 0; u < nt; ++u)
         {
-          const uint64_t i0 = a[u] * TILE, j0 = b[u] * TILE;
-          if (a[u] > b[u] && i0 + TILE <= n && j0 >= row_begin && i0 + TILE <= row_end)
+          const uint64_t i0 = a[u] * TD, j0 = b[u] * TD;
+          if (a[u] > b[u] && i0 + TD <= n && j0 >= row_begin && i0 + TD <= row_end)
           {
             // interior tile with both copies inside the band (the band is
             // contiguous and j0 < i0): plain row-pointer walks
             T* d1 = dense + (i0 + ty - row_begin) * ld + j0 + tx;
             T* d2 = dense + (j0 + ty - row_begin) * ld + i0 + tx;
 #pragma unroll
-            for (int q = 0; q < TILE / ROWS; ++q)
+            for (int q = 0; q < TD / ROWS; ++q)
             {
               const int r = ty + q * ROWS;
               d1[0] = tile[u][r][tx];
@@ -148,7 +155,7 @@ namespace sbg
           }
           // dense tile (a, b): rows of block a inside the band; on the
           // diagonal tile the upper half is the transposed lower half
-          for (int r = ty; r < TILE; r += ROWS)
+          for (int r = ty; r < TD; r += ROWS)
           {
             const uint64_t i = i0 + r, j = j0 + tx;
             if (i >= row_begin && i < row_end && j < n)
@@ -157,7 +164,7 @@ namespace sbg
           // dense tile (b, a), a > b: the transpose
           if (a[u] != b[u])
           {
-            for (int r = ty; r < TILE; r += ROWS)
+            for (int r = ty; r < TD; r += ROWS)
             {
               const uint64_t i = j0 + r, j = i0 + tx;
               if (i >= row_begin && i < row_end && j < n) dense[(i - row_begin) * ld + j] = tile[u][tx][r];
@@ -257,14 +264,6 @@ namespace sbg
       if (f && (threadIdx.x & 31) == 0) atomicOr(flags, f);
     }
 
-    int grid_for(uint64_t tiles)
-    {
-      const DeviceInfo d = device_info();
-      const uint64_t g = (uint64_t)d.sms * 8;  // 8 CTAs of 256 threads per SM
-      tiles = (tiles + 1) / 2;                  // condensed_to_dense takes two tiles per iteration
-      return (int)(tiles < g ? (tiles ? tiles : 1) : g);
-    }
-
     template <typename F>
     int abi_call(F&& f)
     {
@@ -310,19 +309,22 @@ extern "C"
       if (ld < n) throw Error(ST_INVALID_ARGUMENT, "ld must be >= n");
       if (!dense || (!condensed && output_count(skip, n, n) > 0))
         throw Error(ST_INVALID_ARGUMENT, "null matrix pointer");
-      const uint64_t nb = ceil_div_u64(n, TILE);
+      constexpr int TD = C2D_TILE, NT = C2D_TILE == 32 ? 2 : 1;
+      const uint64_t nb = ceil_div_u64(n, TD);
       TileSet ts;
-      ts.init(row_begin / TILE, ceil_div_u64(row_end, TILE), nb);
+      ts.init(row_begin / TD, ceil_div_u64(row_end, TD), nb);
       const bool diag = skip == SBG_SKIP_LOWER;
       cudaStream_t st = (cudaStream_t)stream;
-      const dim3 block(TILE, ROWS);
-      const int grid = grid_for(ts.count);
+      const dim3 block(TD, ROWS);
+      const uint64_t iters = (ts.count + NT - 1) / NT;
+      const int grid = (int)std::min<uint64_t>(std::max<uint64_t>(iters, 1),
+                                               (uint64_t)device_info().sms * (2048 / (TD * ROWS)));
       if (dtype == SBG_F32)
-        condensed_to_dense_kernel<float><<<grid, block, 0, st>>>((const float*)condensed, n, diag, (float*)dense, ld,
-                                                                  row_begin, row_end, ts);
+        condensed_to_dense_kernel<float, TD, NT><<<grid, block, 0, st>>>((const float*)condensed, n, diag,
+                                                                          (float*)dense, ld, row_begin, row_end, ts);
       else
-        condensed_to_dense_kernel<double><<<grid, block, 0, st>>>((const double*)condensed, n, diag, (double*)dense,
-                                                                   ld, row_begin, row_end, ts);
+        condensed_to_dense_kernel<double, TD, NT><<<grid, block, 0, st>>>((const double*)condensed, n, diag,
+                                                                           (double*)dense, ld, row_begin, row_end, ts);
       SBG_CUDA(launched());
     });
   }
