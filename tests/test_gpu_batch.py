@@ -135,3 +135,27 @@ def test_pdist_and_kernel_batched_api():
         assert isinstance(D, sb.DistanceMatrix) and D.size == X.shape[0]
         assert rel_err(D.data, sb.pdist(X).data) <= 1e-5
         assert rel_err(K.data, sb.l2_kernel(X).data, floor=1.0) <= 1e-5
+
+
+@pytest.mark.parametrize("variant", [6, 4])
+def test_batch_f64_windowed_and_hybrid(variant):
+    """Double-precision batches run the hybrid kernel by default; the
+    time-windowed one on request, with a window cap small enough that long
+    PCFs take several windows, against the oracle (float64 1e-12)."""
+    import stablebear_gb300 as sb
+    from stablebear_gb300.batch import PairwiseBatch
+    from oracle import oracle as orc
+    probs = _problems(11, 7, dt=np.float64, nmax=150, lmax=700)
+    sb.set_tuning(variant=variant)
+    sb.set_window_cap(64 if variant == 6 else 0)
+    try:
+        b = PairwiseBatch(probs, op="l2_kernel", graph=False)
+    finally:
+        sb.set_tuning()
+        sb.set_window_cap(0)
+    outs = [o.cpu().numpy() for o in b.run()]
+    for (pts, off), got in zip(probs, outs):
+        if len(off) > 1:
+            want = orc.evaluate(pts, off, op=orc.OP_L2, mode=orc.MODE_KERNEL, truth=True)
+            assert rel_err(got, want, floor=1.0) <= 1e-12
+    b.close()
