@@ -49,6 +49,7 @@ namespace sbg
     T* grad;                // (npts, 2): [dL/dt, dL/dv]
     uint32_t row_cap;       // per-warp shared gradient buffer (elements)
     uint32_t cols_cap;      // staged column elements per lane (0: columns read through L1)
+    const uint32_t* perm;   // processing order -> PCF index (the windowed length order), or null
   };
 
   namespace
@@ -77,10 +78,15 @@ namespace sbg
     }
   }
 
-  // SQUARE: every ordered pair (i, j), i != j, and only the warp's own row
+  // SIDE 0: the lower triangle, both sides take gradients (the row side in
+  // the warp's shared buffer, the column side with global atomics).
+  // SIDE 1: every ordered pair (i, j), i != j, and only the warp's own row
   // side takes gradients (each PCF collects its gradients as the row of its
-  // pairs); no global atomics inside the merge.  Otherwise: the lower
-  // triangle, both sides, the column side with global atomics.
+  // pairs); no global atomics inside the merge.
+  // SIDE 2: every ordered pair, and only the column side takes gradients
+  // (each PCF collects them as a column): every flush is a global vector
+  // reduction to an address no other lane of the warp uses, and no shared
+  // memory atomics remain.
   //
   // WARP_ITEMS: every warp takes its own items from the queue and walks the
   // item's rows itself, so the warps of a CTA work on different column
@@ -100,9 +106,10 @@ namespace sbg
     atomicAdd(p + 1, b);
   }
 
-  template <typename T, int OP, bool SQUARE, bool WARP_ITEMS>
+  template <typename T, int OP, int SIDE, bool WARP_ITEMS>
   __global__ void __launch_bounds__(1024) pairs_backward_kernel(const __grid_constant__ BwdParams<T> B)
   {
+    constexpr bool SQUARE = SIDE != 0, ROWS = SIDE != 2, COLS = SIDE != 1;
     // Shared memory: the item's 32 columns, interleaved (element k of column
     // j at [k * 32 + j]) when cols_cap > 0, then the per-warp row-gradient
     // buffers.
@@ -152,8 +159,11 @@ namespace sbg
       const uint64_t cj = col0 + lane;
       const bool cvalid = cj < B.n;
       const uint64_t cj_eff = cvalid ? cj : col0;
-      const uint64_t coff = B.off[cj_eff];
-      const uint32_t clen = (uint32_t)(B.off[cj_eff + 1] - coff);
+      // the lane's column in the caller's numbering (processing order -> PCF)
+      uint64_t corig = B.perm ? B.perm[cj_eff] : cj_eff;
+      if (corig >= B.n) corig = 0;  // never expected: the order is a permutation
+      const uint64_t coff = B.off[corig];
+      const uint32_t clen = (uint32_t)(B.off[corig + 1] - coff);
       const uint32_t maxlc = __reduce_max_sync(FULL, clen);
       const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > B.npts);
       // the same item for every warp: these are CTA-uniform
@@ -180,14 +190,16 @@ namespace sbg
           }
           const uint64_t i = row_lo + r;
           if (i >= row_hi) break;
-          const uint64_t roff = B.off[i];
-          const uint32_t rlen = (uint32_t)(B.off[i + 1] - roff);
+          const uint64_t iorig = B.perm ? B.perm[i] : i;
+          if (iorig >= B.n) continue;  // never expected: the order is a permutation
+          const uint64_t roff = B.off[iorig];
+          const uint32_t rlen = (uint32_t)(B.off[iorig + 1] - roff);
           if (rlen == 0 || rlen > B.row_cap || roff + rlen > B.npts) continue;
           const bool ok = cvalid && (SQUARE ? cj != i : cj < i);
           T w = T(0);
           if (ok)
           {
-            const uint64_t idx = condensed_index(B.mode, i, cj);
+            const uint64_t idx = condensed_index(B.mode, iorig, corig);
             w = B.grad_out[idx];
             if (OP == BWD_L2DIST)
             {
@@ -197,8 +209,11 @@ namespace sbg
           }
           if (!__any_sync(FULL, w != T(0))) continue;
 
-          for (uint32_t k = lane; k < rlen; k += 32) { sgv[k] = T(0); sgt[k] = T(0); }
-          __syncwarp();
+          if (ROWS)
+          {
+            for (uint32_t k = lane; k < rlen; k += 32) { sgv[k] = T(0); sgt[k] = T(0); }
+            __syncwarp();
+          }
 
           const Elem<T>* row = B.pk + roff;
           Elem<T> F = row[0], Gc = colbase[0];
@@ -226,10 +241,10 @@ namespace sbg
             if (advG) Gn = colbase[(size_t)(gi + 1) * cstride];
             if (w != T(0))
             {
-              if (advF) atomicAdd(&sgv[fi], w * accF);
-              if (advF && !(F.tn == Gc.tn)) atomicAdd(&sgt[fi], w * step_delta<OP>(F.v, Fn.v, Gc.v));
+              if (ROWS && advF) atomicAdd(&sgv[fi], w * accF);
+              if (ROWS && advF && !(F.tn == Gc.tn)) atomicAdd(&sgt[fi], w * step_delta<OP>(F.v, Fn.v, Gc.v));
               // dL/dv of the column element and dL/dt of the next share a slot
-              if (!SQUARE && advG)
+              if (COLS && advG)
                 red_add2(&B.grad[2 * (coff + gi)], w * accG,
                          (Gc.tn == t) ? T(0) : w * step_delta<OP>(Gc.v, Gn.v, F.v));
             }
@@ -241,15 +256,18 @@ namespace sbg
             Gc = Gn;
             t = tn;
           }
-          if (w != T(0)) atomicAdd(&sgv[fi], w * accF);
-          if (!SQUARE && w != T(0)) atomicAdd(&B.grad[2 * (coff + gi)], w * accG);
-          __syncwarp();
-          for (uint32_t k = lane; k < rlen; k += 32)
+          if (ROWS && w != T(0)) atomicAdd(&sgv[fi], w * accF);
+          if (COLS && w != T(0)) atomicAdd(&B.grad[2 * (coff + gi)], w * accG);
+          if (ROWS)
           {
-            const T gv = sgv[k], gt = sgt[k];
-            if (gv != T(0) || gt != T(0)) red_add2(&B.grad[2 * (roff + k)], gv, gt);
+            __syncwarp();
+            for (uint32_t k = lane; k < rlen; k += 32)
+            {
+              const T gv = sgv[k], gt = sgt[k];
+              if (gv != T(0) || gt != T(0)) red_add2(&B.grad[2 * (roff + k)], gv, gt);
+            }
+            __syncwarp();
           }
-          __syncwarp();
         }
       }
       if (!WARP_ITEMS) __syncthreads();
@@ -325,14 +343,20 @@ namespace sbg
     void* packed = nullptr;
     void* queue = nullptr;
     void* paired = nullptr;
+    void* order = nullptr;
     SBG_CUDA(cudaMallocAsync(&packed, std::max<uint64_t>(1, npts) * sizeof(Elem<T>), st));
     SBG_CUDA(cudaMallocAsync(&queue, 256, st));
     SBG_CUDA(cudaMallocAsync(&paired, std::max<uint64_t>(1, npts) * 2 * sizeof(T), st));
+    SBG_CUDA(cudaMallocAsync(&order, n * sizeof(uint32_t), st));
     struct Free
     {
-      void* a; void* b; void* c; cudaStream_t s;
-      ~Free() { cudaFreeAsync(a, s); cudaFreeAsync(b, s); cudaFreeAsync(c, s); }
-    } guard{packed, queue, paired, st};
+      void* a; void* b; void* c; void* d; cudaStream_t s;
+      ~Free() { cudaFreeAsync(a, s); cudaFreeAsync(b, s); cudaFreeAsync(c, s); cudaFreeAsync(d, s); }
+    } guard{packed, queue, paired, order, st};
+    // The forward's processing order (windows of 1024 PCFs by length): the
+    // 32 columns of a group then have similar lengths, so the warp-uniform
+    // step count wastes little.  Gradients land at the PCFs' own offsets.
+    length_order_device(off, n, static_cast<uint32_t*>(order), nullptr, st);
     SBG_CUDA(cudaMemsetAsync(paired, 0, std::max<uint64_t>(1, npts) * 2 * sizeof(T), st));
     SBG_CUDA(launch_pack<T>(pts, off, n, static_cast<Elem<T>*>(packed), npts, dev.sms, st));
 
@@ -342,13 +366,23 @@ namespace sbg
     B.grad_out = grad_out; B.fwd = fwd; B.grad = static_cast<T*>(paired);
     B.queue = static_cast<unsigned long long*>(queue);
     B.row_cap = lmax;
+    B.perm = static_cast<const uint32_t*>(order);
     // As many warps (up to 32) as the per-warp row-gradient buffers allow:
     // the merge is latency-bound, so occupancy pays.  Columns are read
     // through L1: staging them in shared memory (behind
     // SBG_BWD_STAGE_COLUMNS) costs warps and measured slower (N = 4096, L2
     // kernel, forward + backward: 26.4 ms with 24 warps and staged columns
     // against 25.6 ms with 32 warps).
-    const size_t grad_per_warp = (size_t)lmax * 2 * sizeof(T);
+#if defined(SBG_BWD_SQUARE_COLUMNS)
+    constexpr int SIDE = 2;
+#elif defined(SBG_BWD_SQUARE)
+    constexpr int SIDE = 1;
+#else
+    constexpr int SIDE = 0;
+#endif
+    constexpr bool SQ = SIDE != 0;
+    // per-warp row-gradient buffers (none when only columns take gradients)
+    const size_t grad_per_warp = SIDE == 2 ? 0 : (size_t)lmax * 2 * sizeof(T);
     const size_t cols_bytes = (size_t)32 * lmax * sizeof(Elem<T>);
     const size_t budget = dev.smem_optin > 2048 ? dev.smem_optin - 2048 : 0;
 #if defined(SBG_BWD_STAGE_COLUMNS) && !defined(SBG_BWD_WARP_ITEMS)
@@ -363,15 +397,13 @@ namespace sbg
     if (stage) while (warps < 32 && fixed + (size_t)(warps + 8) * grad_per_warp <= budget) warps += 8;
     const size_t smem = fixed + (size_t)warps * grad_per_warp;
     if (smem > budget) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
-    // The ordered-pairs variant measured slower on GB300 (N = 4096, L2 kernel:
-    // forward + backward 74 ms against 46 ms): twice the merges, and the
-    // lanes' shared-memory adds into one row buffer contend.  It stays
-    // available for measurement behind SBG_BWD_SQUARE.
-#ifdef SBG_BWD_SQUARE
-    constexpr bool SQ = true;
-#else
-    constexpr bool SQ = false;
-#endif
+    // The ordered-pairs variants measured slower on GB300 (N = 4096, L2
+    // kernel): rows only, forward + backward 74 ms against 46 ms at the time
+    // (twice the merges, and the lanes' shared-memory adds into one row
+    // buffer contend); columns only, backward 25.7 against 20.8 ms (every
+    // flush a global reduction: the L2 atomic units bound it).  They stay
+    // available for measurement behind SBG_BWD_SQUARE and
+    // SBG_BWD_SQUARE_COLUMNS.
     // Per-warp items measured slower (58 against 50 ms): the column atomics
     // were not colliding; they stay available behind SBG_BWD_WARP_ITEMS.
 #ifdef SBG_BWD_WARP_ITEMS
@@ -390,9 +422,9 @@ namespace sbg
     SBG_CUDA(cudaMemsetAsync(queue, 0, 8, st));
     if (B.total_items > 0)
     {
-      void (*fn)(const BwdParams<T>) = bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SQ, WI>
-                                     : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SQ, WI>
-                                                         : pairs_backward_kernel<T, BWD_L1DIST, SQ, WI>;
+      void (*fn)(const BwdParams<T>) = bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SIDE, WI>
+                                     : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SIDE, WI>
+                                                         : pairs_backward_kernel<T, BWD_L1DIST, SIDE, WI>;
       SBG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms);
       fn<<<grid, warps * 32, smem, st>>>(B);
