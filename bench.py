@@ -689,6 +689,18 @@ def main():
                  "frac": (smem_ach / smem_peak) if smem_peak else None,
                  "work_model": "8 B of (t, v) per lane per merged rectangle, from shared memory",
                  "peak_source": f"128 B/clk/SM x {sms} SMs x sampled SM clock"}
+    # What binds the kernel: shared-memory wavefronts.  A warp-step (one
+    # rectangle per lane) issues three predicated loads, the row's time and
+    # value words (one wavefront each) and the column's 8-byte element (two:
+    # a 64-bit load touches both half-warps); ncu measures 4.2 per warp-step,
+    # at most one wavefront per SM per clock.
+    if mhz:
+        ceiling = sms * mhz * 1e6 * 32 / 4.0
+        smem_view["wavefront_ceiling"] = {
+            "rect_per_s": ceiling, "achieved_rect_per_s": segs / (ms_step / 1e3),
+            "frac": segs / (ms_step / 1e3) / ceiling,
+            "model": "4 shared-memory wavefronts per warp-step of 32 rectangles, 1 wavefront per SM per clock "
+                     f"x {sms} SMs x sampled SM clock"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
