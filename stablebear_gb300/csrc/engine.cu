@@ -262,11 +262,16 @@ namespace sbg
     // less end-of-item idling) while keeping >= 6 items per SM.  At most
     // 1024 rows, one processing-order window, so that bands of whole
     // windows start on item boundaries.
+    // The hybrid kernel reads rows through L1 and restages only its 32
+    // columns per item, so big items buy it little but a ragged tail on
+    // uneven lengths: at most 64 rows (f64 stable-rank N = 20,000, L2 kernel
+    // / pdist: 1921 / 2458 ms against 2048 / 2533 ms with 1024 rows).
+    const uint32_t q_top = pl.kvar == 3 ? 2u : 32u;
     uint32_t q = (uint32_t)std::max(0, settings().rowChunk.load());
     if (q == 0)
     {
       q = 1;
-      for (uint32_t cand = 32; cand >= 1; cand /= 2)
+      for (uint32_t cand = q_top; cand >= 1; cand /= 2)
       {
         if (items_for(mode, 0, nr, nc, cand) >= (uint64_t)dev.sms * 6) { q = cand; break; }
       }
