@@ -97,6 +97,18 @@ def test_settings_roundtrip(lib):
     assert lib.sbg_get_force_cpu() == 1
     sb.force_cpu(False)
     sb.set_tuning()
+    # the time-windowed variant and its window cap
+    assert lib.sbg_set_tuning(0, 0, 6, 0, 0) == 0
+    assert lib.sbg_set_tuning(0, 0, 7, 0, 0) == -1
+    assert b"variant" in lib.sbg_last_error()
+    sb.set_window_cap(40)
+    assert sb.get_window_cap() == 40
+    assert lib.sbg_set_window_cap(-1) == -1
+    assert lib.sbg_set_window_cap((1 << 20) + 1) == -1
+    assert b"window cap" in lib.sbg_last_error()
+    assert sb.get_window_cap() == 40
+    sb.set_window_cap(0)
+    sb.set_tuning()
 
 
 def _items(lib, mode, nr, nc, rb, re, q):
