@@ -133,6 +133,21 @@ class _Condensed:
     def __eq__(self, other):
         return type(other) is type(self) and self._n == other._n and np.array_equal(self._data, other._data)
 
+    def allclose(self, other, atol=1e-8, rtol=1e-5) -> bool:
+        """Whether every stored element satisfies ``|a - b| <= atol + rtol |b|``
+        (b from ``other``), evaluated in the element type; False when the
+        storage sizes differ.  As in the reference
+        (include/sbear/tensor.tpp:1702-1718, bound in
+        src/python/py_distance_matrix.hpp:76-78), an element fails only when
+        the difference exceeds the tolerance, so NaN entries do not fail."""
+        if type(other) is not type(self) or other._data.dtype != self._data.dtype:
+            raise TypeError(f"allclose needs another {type(self).__name__} of the same element type")
+        a, b = self._data, other._data
+        if a.shape != b.shape:
+            return False
+        dt = a.dtype
+        return not bool(np.any(np.abs(a - b) > dt.type(atol) + dt.type(rtol) * np.abs(b)))
+
     def __repr__(self):
         # as the reference's bound classes print (py_distance_matrix.hpp:78-83)
         suffix = "_f32" if self._data.dtype == np.float32 else "_f64"

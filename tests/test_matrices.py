@@ -101,3 +101,39 @@ def test_from_dense_messages():
 def test_repr_as_the_reference():
     assert repr(sb.DistanceMatrix(3, dtype=np.float32)) == "DistanceMatrix_f32(size=3)"
     assert repr(sb.SymmetricMatrix(4)) == "SymmetricMatrix_f64(size=4)"
+
+
+def test_allclose_as_the_reference():
+    """allclose: |a - b| <= atol + rtol |b| element-wise, in the element type
+    (include/sbear/tensor.tpp:1687-1718); matrices compare their storage and
+    let NaN entries pass, dense arrays do not."""
+    import stablebear_gb300 as sb
+    a = sb.DistanceMatrix(4, dtype=np.float32)
+    a.data[:] = np.arange(1, 7, dtype=np.float32)
+    b = a.copy()
+    assert sb.allclose(a, b) and a.allclose(b)
+    b.data[3] += np.float32(1e-4)  # |a - b| = 1e-4 > 1e-8 + 1e-5 * 4.0001
+    assert not sb.allclose(a, b)
+    assert sb.allclose(a, b, rtol=1e-4)
+    assert sb.allclose(a, b, atol=1e-4)
+    b = a.copy()
+    b.data[0] = np.nan
+    assert sb.allclose(a, b)  # a NaN does not exceed the tolerance
+    assert not sb.allclose(a, sb.DistanceMatrix(5, dtype=np.float32))
+    with pytest.raises(TypeError):
+        sb.allclose(a, sb.SymmetricMatrix(4, dtype=np.float32))
+    with pytest.raises(TypeError):
+        a.allclose(sb.DistanceMatrix(4, dtype=np.float64))
+    k = sb.SymmetricMatrix(3, dtype=np.float64)
+    k.data[:] = 1.0
+    k2 = k.copy()
+    k2.data[:] += 5e-6
+    assert sb.allclose(k, k2) and not sb.allclose(k, k2, rtol=1e-6)
+    x = np.ones((2, 3), np.float32)
+    y = x.copy()
+    assert sb.allclose(x, y)
+    y[0, 0] = np.nan
+    assert not sb.allclose(x, y)  # dense arrays: a NaN fails
+    assert not sb.allclose(x, np.ones((3, 2), np.float32))
+    with pytest.raises(TypeError):
+        sb.allclose(x, a)
