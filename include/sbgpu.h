@@ -53,7 +53,8 @@ typedef enum sbg_status {
   SBG_ERR_LOGIC = -9            /* logic_error (cuda_result_writer.hpp:63-90) */
 } sbg_status;
 
-typedef enum sbg_dtype { SBG_F32 = 0, SBG_F64 = 1 } sbg_dtype;
+typedef enum sbg_dtype { SBG_F32 = 0, SBG_F64 = 1, SBG_I32 = 2, SBG_I64 = 3 } sbg_dtype;
+/* (SBG_I32 / SBG_I64: integer-valued PCFs, taken by sbg_iterate_rectangles only) */
 
 /* Pair operations (include/sbear/functional/operations.cuh:19-65). */
 typedef enum sbg_op { SBG_OP_L1 = 0, SBG_OP_LP = 1, SBG_OP_L2_INNER = 2 } sbg_op;
@@ -213,6 +214,20 @@ int sbg_pairwise_backward_device(int dtype, int op, double p, int skip_mode,
                                  const void* points, const uint64_t* offsets, uint64_t n, uint64_t n_points,
                                  uint32_t max_points, const void* grad_out, const void* forward_out,
                                  void* grad_points, void* stream);
+
+/* ---- the rectangles of one pair --------------------------------------------------
+ * Replaces sb::iterate_rectangles (include/sbear/algorithms/functional/iterate_rectangles.hpp:37-104)
+ * as bound for Python (src/python/functional/py_pcf.cpp:92-96, the Backend_*::iterate_rectangles of
+ * stablebear.iterate_rectangles, stablebear/functional/pcf.py:347-374): the intervals [left, right)
+ * on which both PCFs are constant, in time order, from the last breakpoint at or before a (the first
+ * if none) up to b, each with f's and g's value there.  f_points / g_points: host arrays of nf / ng
+ * interleaved (t, v) points of the dtype (SBG_F32, SBG_F64, SBG_I32, SBG_I64), times sorted.  a and
+ * b are converted to the dtype (for integer types, infinities to its limits).  Writes up to cap
+ * rectangles as (left, right, f_value, g_value) of the dtype into out and the number of rectangles
+ * (all of them, also past cap; at most nf + ng - 1) into *count.  Runs on the current device and
+ * returns when the result is on the host. */
+int sbg_iterate_rectangles(int dtype, const void* f_points, uint64_t nf, const void* g_points, uint64_t ng,
+                           double a, double b, void* out, uint64_t cap, uint64_t* count);
 
 /* ---- batches: many independent problems in one persistent launch ----------------
  * No single counterpart in the reference (it runs one problem per task); each

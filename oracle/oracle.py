@@ -394,3 +394,43 @@ def ref_gpu_triangle(dev_points_ptr, dev_offsets_ptr, n, *, op="l1", p=1.0, kern
     if rc != 0:
         raise RuntimeError(err.value.decode())
     return ms.value, int(tiles.value)
+
+
+def rectangles(f, g, a=0.0, b=float("inf")):
+    """The reference's rectangle walk for one pair, restated as a plain loop
+    (include/sbear/algorithms/functional/iterate_rectangles.hpp:23-104):
+    both sides start at their last point at or before a (the first point if
+    none); while t < b the side with the earlier next breakpoint advances
+    (both on a tie), and each step emits (tprev, min(max(f.t, g.t), b),
+    f value, g value); once both are exhausted the last rectangle runs to b.
+    f, g: (n, 2) arrays of (t, v).  Returns an (m, 4) array."""
+    f = np.asarray(f)
+    g = np.asarray(g)
+
+    def start(p):
+        i = int(np.searchsorted(p[:, 0], a, side="right"))
+        return 0 if i == 0 else i - 1
+
+    fi, gi = start(f), start(g)
+    t = tprev = a
+    out = []
+    while t < b:
+        tprev = t
+        fv, gv = f[fi, 1], g[gi, 1]
+        fn, gn = fi + 1 < len(f), gi + 1 < len(g)
+        if fn and gn:
+            delta = f[fi + 1, 0] - g[gi + 1, 0]
+            if delta <= 0:
+                fi += 1
+            if delta >= 0:
+                gi += 1
+        elif fn:
+            fi += 1
+        elif gn:
+            gi += 1
+        else:
+            out.append((tprev, b, fv, gv))
+            break
+        t = min(max(f[fi, 0], g[gi, 0]), b)
+        out.append((tprev, t, fv, gv))
+    return np.array(out, dtype=np.float64).reshape(-1, 4)

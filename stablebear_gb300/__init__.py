@@ -10,6 +10,7 @@ behind the C ABI declared in ``include/sbgpu.h``; there is no CPU fallback.
 from .pcf import Pcf, PcfArray, pcf32, pcf64, pcf32i, pcf64i, float32, float64, zeros
 from .matrices import DistanceMatrix, SymmetricMatrix
 from .comparison import allclose
+from .rectangles import Rectangle, iterate_rectangles
 from .distance import (
     pdist, cdist, l2_kernel, lp_distance,
     Distance_f32_f32, Distance_f64_f64, InnerProduct_f32_f32, InnerProduct_f64_f64,
@@ -25,7 +26,7 @@ from . import persistence
 
 __all__ = [
     "Pcf", "PcfArray", "pcf32", "pcf64", "pcf32i", "pcf64i", "float32", "float64", "zeros",
-    "DistanceMatrix", "SymmetricMatrix", "allclose",
+    "DistanceMatrix", "SymmetricMatrix", "allclose", "Rectangle", "iterate_rectangles",
     "pdist", "cdist", "l2_kernel", "lp_distance",
     "Distance_f32_f32", "Distance_f64_f64", "InnerProduct_f32_f32", "InnerProduct_f64_f64",
     "force_cpu", "set_block_size", "limit_cpus", "limit_gpus", "set_cuda_threshold", "get_cuda_threshold",

@@ -27,6 +27,7 @@ STATUS_NAMES = {
 }
 
 F32, F64 = 0, 1
+I32, I64 = 2, 3  # integer PCFs (sbg_iterate_rectangles)
 OP_L1, OP_LP, OP_L2_INNER = 0, 1, 2
 SKIP_NONE, SKIP_LOWER_NODIAG, SKIP_LOWER = 0, 1, 2
 FLAG_ASYMMETRIC, FLAG_DIAGONAL, FLAG_NEGATIVE = 1, 2, 4  # sbg_dense_to_condensed_device
@@ -87,6 +88,7 @@ SIGNATURES = {
     "sbg_dense_to_condensed_device": (_I, [_I, _I, _U64, _P, _U64, _P, _P, _P]),
     "sbg_lp_norm_device": (_I, [_I, _D, _P, _P, _U64, _P, _P]),
     "sbg_lp_norm_host": (_I, [_I, _D, _P, _P, _U64, _P]),
+    "sbg_iterate_rectangles": (_I, [_I, _P, _U64, _P, _U64, _D, _D, _P, _U64, _P]),
     "sbg_barcode_pcf_capacity": (_U64, [_I, _U64, _U64]),
     "sbg_barcodes_to_pcfs_device": (_I, [_I, _I, _P, _P, _U64, _U64, _P, _U64, _P, _P]),
     "sbg_barcodes_to_pcfs_host": (_I, [_I, _I, _P, _P, _U64, _P, _U64, _P]),

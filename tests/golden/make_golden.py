@@ -102,6 +102,7 @@ def main():
         "start_late": orc.ref_rectangles(f, g, 2.0),
     }
     np.savez(os.path.join(HERE, "reference_rectangles.npz"), f=f, g=g, **rects)
+    rectangle_cases()
 
     # CudaBlockScheduler blocks for a few configurations.
     sched = {}
@@ -144,5 +145,37 @@ def main():
     np.savez(os.path.join(HERE, "reference_norms.npz"), **norms)
 
 
+def rectangle_cases():
+    """The reference's rectangle walk on seeded random pairs with repeated
+    times (zero-width segments), breakpoints shared by f and g, and bounds
+    before, on and between breakpoints.  Times and values are multiples of
+    1/2 below 64, exact in float32 as well."""
+    from oracle import oracle as orc
+    rng = np.random.default_rng(77)
+    out = {}
+    for k in range(40):
+        def pcf():
+            n = int(rng.integers(1, 13))
+            t = np.concatenate([[0.0], np.cumsum(rng.choice([0.0, 0.5, 1.0, 1.5], size=n - 1))])
+            v = rng.integers(-4, 5, size=n).astype(np.float64)
+            return np.stack([t, v], 1)
+        f, g = pcf(), pcf()
+        if k % 3 == 0 and len(f) > 2:  # share some of f's breakpoints with g
+            g = np.concatenate([g, f[1:3]])
+            g = g[np.argsort(g[:, 0], kind="stable")]
+            g[0, 0] = 0.0
+        a = float(rng.choice([0.0, 0.0, 0.5, 1.25, 3.0, -1.0]))
+        b = float(rng.choice([np.finfo(np.float64).max, 2.5, 4.0, 100.0, a]))
+        out[f"f_{k}"], out[f"g_{k}"] = f, g
+        out[f"ab_{k}"] = np.array([a, b])
+        out[f"rects_{k}"] = orc.ref_rectangles(f, g, a, b)
+    path = os.path.join(HERE, "reference_rectangle_cases.npz")
+    np.savez(path, **out)
+    print(path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
+    if "--rectangles" in sys.argv:
+        rectangle_cases()
+        sys.exit(0)
     main()

@@ -264,3 +264,17 @@ def test_betti_curve_known_answers():
         assert _summary([[0, 2], [1, 3], [0.5, 1.5]], 1, dt) == [[0, 1], [0.5, 2], [1, 3], [1.5, 2], [2, 1], [3, 0]]
         assert _summary([[0, 1], [0, 2], [0, 3]], 1, dt) == [[0, 3], [1, 2], [2, 1], [3, 0]]
         assert _summary([[0, np.inf], [1, 2]], 1, dt) == [[0, 1], [1, 2], [2, 1]]
+
+
+def test_rectangle_walk_restatement_matches_reference_cases():
+    """The oracle's rectangle walk against the reference's own walk, recorded
+    on random pairs with repeated and shared breakpoints and assorted bounds
+    (tests/golden/make_golden.py rectangle_cases)."""
+    d = np.load(os.path.join(GOLDEN, "reference_rectangle_cases.npz"))
+    k = 0
+    while f"f_{k}" in d.files:
+        a, b = d[f"ab_{k}"]
+        got = orc.rectangles(d[f"f_{k}"], d[f"g_{k}"], a, b)
+        np.testing.assert_array_equal(got, d[f"rects_{k}"])
+        k += 1
+    assert k == 40
