@@ -54,9 +54,37 @@ static void run(const char* tag)
   std::printf("%s range_rejected %d\n", tag, rejected ? 1 : 0);
 }
 
+// The reference's known answers (test/test_l1_dist.cu:98-124): two
+// default-constructed PCFs are at distance 0, and {(0,3),(1,0)} against
+// {(0,1),(2,0)} at L1 distance 3, read back through operator() both ways.
+template <typename T>
+static void known_answers(const char* tag)
+{
+  using P = sb::TimePoint<T, T>;
+  std::vector<sb::Pcf<T, T>> empty;
+  empty.resize(2);
+  sb::DistanceMatrix<T> d0(2);
+  auto t0 = sb::create_cuda_block_integrate_l1_task(d0, empty);
+  t0->start_async(0);
+  t0->wait();
+  std::printf("%s kat_empty %.17g\n", tag, (double)T(d0(0, 1)));
+
+  std::vector<sb::Pcf<T, T>> two;
+  two.emplace_back(std::vector<P>{{T(0), T(3)}, {T(1), T(0)}});
+  two.emplace_back(std::vector<P>{{T(0), T(1)}, {T(2), T(0)}});
+  sb::DistanceMatrix<T> d1(2);
+  auto t1 = sb::create_cuda_block_integrate_l1_task(d1, two);
+  t1->start_async(0);
+  t1->wait();
+  std::printf("%s kat_two %.17g %.17g %.17g %.17g\n", tag, (double)T(d1(0, 0)), (double)T(d1(0, 1)),
+              (double)T(d1(1, 0)), (double)T(d1(1, 1)));
+}
+
 int main()
 {
   run<float>("f32");
   run<double>("f64");
+  known_answers<float>("f32");
+  known_answers<double>("f64");
   return 0;
 }

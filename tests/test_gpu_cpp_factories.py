@@ -32,8 +32,8 @@ def test_factories_match_oracle(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     got = {}
     for ln in r.stdout.splitlines():
-        tag, key, val = ln.split()
-        got.setdefault((tag, key), []).append(float(val))
+        tag, key, *vals = ln.split()
+        got.setdefault((tag, key), []).extend(float(v) for v in vals)
     for tag, dt, tol in (("f32", np.float32, 1e-5), ("f64", np.float64, 1e-12)):
         pts, off = _five(dt)
         cp, co = pts[int(off[2]):], (off[2:] - off[2]).astype(np.uint64)
@@ -53,3 +53,6 @@ def test_factories_match_oracle(tmp_path):
             rel = np.abs(g[fin] - w[fin]) / np.maximum(np.abs(w[fin]), 1.0 if key == "k" else 1e-30)
             assert rel.max() <= tol, (tag, key, g, w)
         assert got[(tag, "range_rejected")] == [1.0]
+        # the reference's known answers (test/test_l1_dist.cu:98-124), exact
+        assert got[(tag, "kat_empty")] == [0.0]
+        assert got[(tag, "kat_two")] == [0.0, 3.0, 3.0, 0.0]
