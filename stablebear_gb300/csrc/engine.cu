@@ -123,27 +123,55 @@ namespace sbg
     if (s.n == 0) return;
     if (!s.off || !s.pts) throw Error(ST_INVALID_ARGUMENT, std::string(what) + ": null points/offsets");
     if (s.off[0] != 0) throw Error(ST_INVALID_INPUT, std::string(what) + ": offsets must start at 0");
-    for (uint64_t i = 0; i < s.n; ++i)
-    {
-      const uint64_t a = s.off[i], b = s.off[i + 1];
-      if (b <= a)
-        throw Error(ST_INVALID_INPUT, std::string(what) + ": PCF " + std::to_string(i) + " has no breakpoints");
-      if (b - a > 0xffffffffull)
-        throw Error(ST_INVALID_INPUT, std::string(what) + ": PCF " + std::to_string(i) + " is too long");
-      const T* p = s.pts + 2 * a;
-      if (p[0] != T(0))
-        throw Error(ST_INVALID_INPUT, std::string(what) + ": PCF " + std::to_string(i)
-                    + ": the first breakpoint must have time t=0 (got t=" + std::to_string((double)p[0]) + ").");
-      for (uint64_t k = 0; k < b - a; ++k)
+    // PCFs [i0, i1): the first invalid one, or i1; its error in *msg.
+    auto check = [&s, what](uint64_t i0, uint64_t i1, std::string* msg) -> uint64_t {
+      for (uint64_t i = i0; i < i1; ++i)
       {
-        const T t = p[2 * k];
-        if (!std::isfinite(t))
-          throw Error(ST_INVALID_INPUT, std::string(what) + ": PCF " + std::to_string(i) + ": breakpoint times must be finite");
-        if (k > 0 && !(p[2 * (k - 1)] <= t))
-          throw Error(ST_INVALID_INPUT, std::string(what) + ": PCF " + std::to_string(i)
-                      + ": Breakpoints must be given in non-decreasing time order.");
+        const uint64_t a = s.off[i], b = s.off[i + 1];
+        if (b <= a) { *msg = std::string(what) + ": PCF " + std::to_string(i) + " has no breakpoints"; return i; }
+        if (b - a > 0xffffffffull) { *msg = std::string(what) + ": PCF " + std::to_string(i) + " is too long"; return i; }
+        const T* p = s.pts + 2 * a;
+        if (p[0] != T(0))
+        {
+          *msg = std::string(what) + ": PCF " + std::to_string(i) +
+                 ": the first breakpoint must have time t=0 (got t=" + std::to_string((double)p[0]) + ").";
+          return i;
+        }
+        for (uint64_t k = 0; k < b - a; ++k)
+        {
+          const T t = p[2 * k];
+          if (!std::isfinite(t))
+          {
+            *msg = std::string(what) + ": PCF " + std::to_string(i) + ": breakpoint times must be finite";
+            return i;
+          }
+          if (k > 0 && !(p[2 * (k - 1)] <= t))
+          {
+            *msg = std::string(what) + ": PCF " + std::to_string(i) + ": Breakpoints must be given in non-decreasing time order.";
+            return i;
+          }
+        }
       }
+      return i1;
+    };
+    // Large inputs are checked in parallel over contiguous ranges of PCFs;
+    // the error reported is the first invalid PCF's, as in a serial scan.
+    const unsigned parts = s.off[s.n] >= (1ull << 20) && s.n >= 1024 ? host_parts() : 1u;
+    if (parts <= 1)
+    {
+      std::string msg;
+      if (check(0, s.n, &msg) < s.n) throw Error(ST_INVALID_INPUT, msg);
+      return;
     }
+    std::vector<uint64_t> bad(parts, ~0ull);
+    std::vector<std::string> msgs(parts);
+    host_parallel([&](unsigned k) {
+      const uint64_t i0 = s.n * k / parts, i1 = s.n * (k + 1) / parts;
+      const uint64_t r = check(i0, i1, &msgs[k]);
+      if (r < i1) bad[k] = r;
+    });
+    for (unsigned k = 0; k < parts; ++k)
+      if (bad[k] != ~0ull) throw Error(ST_INVALID_INPUT, msgs[k]);
   }
 
   template void validate_pcfs<float>(const PcfSet<float>&, const char*);
@@ -195,26 +223,43 @@ namespace sbg
     const size_t usable = dev.smem_optin > reserve ? dev.smem_optin - reserve : 0;
     const uint32_t lmax_c = std::max<uint32_t>(cs.lmax, 1);
     const uint32_t lmax_r = std::max<uint32_t>(rs.lmax, 1);
-    const uint32_t row_cap = lmax_r + lmax_c + (uint32_t)U + 1;
+    const int variant = settings().variant.load();
+    // Row buffer: the row, then sentinel copies for the advances past its
+    // end.  The default walk (variant 5) pulls the row address back every
+    // block, so U copies do; the others need one per step of the longest
+    // column.
+#ifndef SBG_ROW_PAD_FULL
+    const bool short_pad = variant == 0 || variant == 5;
+#else
+    const bool short_pad = false;
+#endif
+    const uint32_t row_cap_full = lmax_r + lmax_c + (uint32_t)U + 1;
+    const uint32_t row_cap = short_pad ? lmax_r + (uint32_t)U + 1 : row_cap_full;
     auto smem_for = [&](int w) { return (size_t)32 * lmax_c * es + (size_t)w * row_cap * es; };
 
-    const int variant = settings().variant.load();
     const int want_w = settings().warps.load();
     // Shared-memory variants (rows and columns staged): the most warps that fit.
-    int warps = 0;
-    if (variant == 0 || variant == 1 || variant == 3 || variant == 5)
-    {
+    auto most_warps = [&](uint32_t cap) {
       const int cands[] = {32, 24, 16, 12, 8, 4};
       for (int w : cands)
       {
         if (want_w > 0 && w > want_w) continue;
-        if (smem_for(w) <= usable) { warps = w; break; }
+        if ((size_t)32 * lmax_c * es + (size_t)w * cap * es <= usable) return w;
       }
-    }
+      return 0;
+    };
+    int warps = 0;
+    if (variant == 0 || variant == 1 || variant == 3 || variant == 5) warps = most_warps(row_cap);
     if ((variant == 1 || variant == 3 || variant == 5) && warps == 0)
       throw Error(ST_INVALID_ARGUMENT, "shared-memory variant requested but the PCFs do not fit in shared memory");
+    // The automatic choice between this kernel and the time-windowed one is
+    // made on the layout with full row padding (at least 16 warps): with the
+    // short padding, L ~ U{16..512} also fits 16 warps, but there (N = 4096)
+    // the plain kernel measured 2.89 / 2.95 ms against 2.86 / 2.88 ms for the
+    // windowed one (L2 kernel / L2 distance).
+    const bool plain_auto = variant == 0 && most_warps(row_cap_full) >= 16;
 
-    if ((variant == 0 && warps >= 16) || variant == 1 || variant == 3 || variant == 5)
+    if (plain_auto || variant == 1 || variant == 3 || variant == 5)
     {
       pl.smem = true;
       pl.packed = false;
@@ -651,7 +696,7 @@ namespace sbg
         const uint64_t npts = h.n ? h.off[h.n] : 0;
         pts.reset(std::max<uint64_t>(1, npts) * 2 * sizeof(T));
         off.reset((h.n + 1) * sizeof(uint64_t));
-        if (npts) SBG_CUDA(cudaMemcpyAsync(pts.get(), h.pts, npts * 2 * sizeof(T), cudaMemcpyHostToDevice, s));
+        if (npts) upload_pageable(pts.get(), h.pts, npts * 2 * sizeof(T), s);
         SBG_CUDA(cudaMemcpyAsync(off.get(), h.off, (h.n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
         view.pts = pts.as<T>();
         view.off = off.as<uint64_t>();

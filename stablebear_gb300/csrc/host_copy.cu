@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -19,7 +20,8 @@ namespace sbg
 {
   namespace
   {
-    // Fixed pool of copy threads; parallel_copy splits one memcpy over them.
+    // Fixed pool of host threads.  run() splits one job into parts, one per
+    // thread plus the caller, and returns when every part is done.
     class CopyPool
     {
     public:
@@ -29,31 +31,44 @@ namespace sbg
         return pool;
       }
 
+      unsigned parts() const { return (unsigned)m_threads.size() + 1; }
+
+      // job(part) for part in [0, parts()); the caller runs the last part.
+      void run(const std::function<void(unsigned)>& job)
+      {
+        if (m_threads.empty())
+        {
+          job(0);
+          return;
+        }
+        std::unique_lock<std::mutex> call(m_call);  // one job at a time
+        {
+          std::lock_guard<std::mutex> lk(m_mu);
+          m_job = &job;
+          m_pending = m_threads.size();
+          ++m_gen;
+        }
+        m_cv.notify_all();
+        job((unsigned)m_threads.size());
+        std::unique_lock<std::mutex> lk(m_mu);
+        m_done.wait(lk, [this] { return m_pending == 0; });
+        m_job = nullptr;
+      }
+
       void copy(void* dst, const void* src, size_t bytes)
       {
-        const size_t nt = m_threads.size() + 1;
+        const size_t nt = parts();
         if (bytes < (8u << 20) || nt == 1)
         {
           std::memcpy(dst, src, bytes);
           return;
         }
-        std::unique_lock<std::mutex> call(m_call);  // one parallel copy at a time
         const size_t part = ((bytes / nt) + 4095) & ~size_t(4095);
-        {
-          std::lock_guard<std::mutex> lk(m_mu);
-          m_dst = static_cast<char*>(dst);
-          m_src = static_cast<const char*>(src);
-          m_bytes = bytes;
-          m_part = part;
-          m_pending = m_threads.size();
-          ++m_gen;
-        }
-        m_cv.notify_all();
-        // the calling thread takes the last part
-        const size_t off = part * m_threads.size();
-        if (off < bytes) std::memcpy(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, bytes - off);
-        std::unique_lock<std::mutex> lk(m_mu);
-        m_done.wait(lk, [this] { return m_pending == 0; });
+        run([&](unsigned k) {
+          const size_t off = part * k;
+          if (off < bytes)
+            std::memcpy(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, std::min(part, bytes - off));
+        });
       }
 
     private:
@@ -61,7 +76,7 @@ namespace sbg
       {
         unsigned hc = std::thread::hardware_concurrency();
         unsigned n = hc > 1 ? std::min(hc, 32u) - 1 : 0;
-        for (unsigned i = 0; i < n; ++i) m_threads.emplace_back([this, i] { run(i); });
+        for (unsigned i = 0; i < n; ++i) m_threads.emplace_back([this, i] { work(i); });
       }
       ~CopyPool()
       {
@@ -74,23 +89,20 @@ namespace sbg
         for (auto& t : m_threads) t.join();
       }
 
-      void run(unsigned idx)
+      void work(unsigned idx)
       {
         uint64_t seen = 0;
         for (;;)
         {
-          char* dst;
-          const char* src;
-          size_t bytes, part;
+          const std::function<void(unsigned)>* job;
           {
             std::unique_lock<std::mutex> lk(m_mu);
             m_cv.wait(lk, [&] { return m_gen != seen; });
             seen = m_gen;
             if (m_quit) return;
-            dst = m_dst; src = m_src; bytes = m_bytes; part = m_part;
+            job = m_job;
           }
-          const size_t off = part * idx;
-          if (off < bytes) std::memcpy(dst + off, src + off, std::min(part, bytes - off));
+          (*job)(idx);
           {
             std::lock_guard<std::mutex> lk(m_mu);
             if (--m_pending == 0) m_done.notify_all();
@@ -101,9 +113,8 @@ namespace sbg
       std::vector<std::thread> m_threads;
       std::mutex m_mu, m_call;
       std::condition_variable m_cv, m_done;
-      char* m_dst = nullptr;
-      const char* m_src = nullptr;
-      size_t m_bytes = 0, m_part = 0, m_pending = 0;
+      const std::function<void(unsigned)>* m_job = nullptr;
+      size_t m_pending = 0;
       uint64_t m_gen = 0;
       bool m_quit = false;
     };
@@ -198,6 +209,67 @@ namespace sbg
   }
 
   void HostStager::flush() { finish_pending(); }
+
+  unsigned host_parts() { return CopyPool::get().parts(); }
+
+  void host_parallel(const std::function<void(unsigned)>& job) { CopyPool::get().run(job); }
+
+  namespace
+  {
+    // Two pinned buffers for uploads, allocated on first use and reused.
+    struct UploadPool
+    {
+      static constexpr size_t CHUNK = 32u << 20;
+      std::mutex mu;
+      void* buf[2] = {nullptr, nullptr};
+      cudaEvent_t ev[2] = {nullptr, nullptr};
+    };
+    UploadPool& upload_pool()
+    {
+      static UploadPool p;
+      return p;
+    }
+  }
+
+  void upload_pageable(void* dev_dst, const void* host_src, size_t bytes, cudaStream_t st)
+  {
+    UploadPool& p = upload_pool();
+    std::unique_lock<std::mutex> lk(p.mu, std::try_to_lock);
+    if (bytes < (16u << 20) || !lk.owns_lock())
+    {
+      // small, or another thread holds the buffers: the driver's own path
+      SBG_CUDA(cudaMemcpyAsync(dev_dst, host_src, bytes, cudaMemcpyHostToDevice, st));
+      return;
+    }
+    if (!p.buf[0])
+    {
+      for (int k = 0; k < 2; ++k)
+      {
+        SBG_CUDA(cudaHostAlloc(&p.buf[k], UploadPool::CHUNK, cudaHostAllocDefault));
+        SBG_CUDA(cudaEventCreateWithFlags(&p.ev[k], cudaEventDisableTiming));
+        SBG_CUDA(cudaEventRecord(p.ev[k], st));
+      }
+    }
+    char* dst = static_cast<char*>(dev_dst);
+    const char* src = static_cast<const char*>(host_src);
+    int slot = 0;
+    while (bytes > 0)
+    {
+      const size_t n = std::min(bytes, UploadPool::CHUNK);
+      // the slot's previous DMA has read the buffer
+      SBG_CUDA(cudaEventSynchronize(p.ev[slot]));
+      CopyPool::get().copy(p.buf[slot], src, n);
+      SBG_CUDA(cudaMemcpyAsync(dst, p.buf[slot], n, cudaMemcpyHostToDevice, st));
+      SBG_CUDA(cudaEventRecord(p.ev[slot], st));
+      slot ^= 1;
+      dst += n;
+      src += n;
+      bytes -= n;
+    }
+    // the buffers are reused by the next upload: wait for the last DMAs
+    SBG_CUDA(cudaEventSynchronize(p.ev[0]));
+    SBG_CUDA(cudaEventSynchronize(p.ev[1]));
+  }
 
   void host_memory_access(int* pageable, int* host_page_tables)
   {

@@ -3,6 +3,8 @@
 
 #include "sbg_internal.hpp"
 
+#include <functional>
+
 namespace sbg
 {
   class HostStager
@@ -31,6 +33,16 @@ namespace sbg
     void* m_pending_dst = nullptr;
     size_t m_pending_bytes = 0;
   };
+
+  // Host -> device copy from pageable host memory (16 MB and up): chunks
+  // are copied by the host thread pool into two pinned buffers while the
+  // previous chunk's DMA runs.  Returns when the data is on the device.
+  void upload_pageable(void* dev_dst, const void* host_src, size_t bytes, cudaStream_t st);
+
+  // The host thread pool: host_parallel(job) runs job(part) for every part
+  // in [0, host_parts()) and returns when all are done.
+  unsigned host_parts();
+  void host_parallel(const std::function<void(unsigned)>& job);
 
   // cudaDevAttrPageableMemoryAccess / ...UsesHostPageTables of the current
   // device: 1/1 on coherent hosts (Grace + NVLink-C2C) where kernels may

@@ -8,17 +8,15 @@
 namespace sbg
 {
   // Rectangles per naive block sum (blocks are combined with Kahan
-  // compensation): 8 for float; 16 for double, where the compensation's four
-  // FP64 adds cost more than a longer naive block loses (f64 sums of 16 terms
-  // stay far below the 1e-12 target).
+  // compensation): 8 for float; 64 for double, whose kernels are bound by the
+  // FP64 pipe, so the compensation's four FP64 operations per block cost a
+  // share of the time that a longer block cuts (a naive block of 64 doubles
+  // errs by at most 63 ulp, far below the 1e-12 target).
   template <typename T> struct Unroll;
 #ifndef SBG_F32_UNROLL
 #define SBG_F32_UNROLL 8
 #endif
   template <> struct Unroll<float> { static constexpr int value = SBG_F32_UNROLL; };
-// Rectangles per naive block between Kahan steps.  The f64 kernels are bound
-// by the FP64 pipe, so a longer block saves a larger share of their FP64
-// work (a naive block of 64 doubles still errs by at most 63 ulp).
 #ifndef SBG_F64_UNROLL
 #define SBG_F64_UNROLL 64
 #endif
@@ -200,18 +198,29 @@ namespace sbg
   }
 
   // ft0: the warp's row times; the values follow `voff` bytes later.
+  // rlen: the row's elements.  Once a lane's pair is done both sides sit on
+  // their sentinels and the row advances on every step; at each block start
+  // the row address is pulled back to the row's last element (the sentinel
+  // itself, equal to every padding copy), so within a block it runs at most
+  // U elements past it and the row buffer needs only U padding copies, not
+  // one per step the longest column of the warp may still take.
   template <typename T, int K, int U>
-  __device__ __forceinline__ T merge_smem_soa(const T* ft0, uint32_t voff, const Elem<T>* pg, uint32_t steps, T p)
+  __device__ __forceinline__ T merge_smem_soa(const T* ft0, uint32_t voff, const Elem<T>* pg, uint32_t steps,
+                                              uint32_t rlen, T p)
   {
     T fv = *reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(ft0) + voff);
     T ft = *ft0;
     Elem<T> G = *pg;
     uint32_t af = (uint32_t)__cvta_generic_to_shared(ft0);
+    const uint32_t af_last = af + (rlen - 1) * (uint32_t)sizeof(T);
     uint32_t ag = (uint32_t)__cvta_generic_to_shared(pg);
     T t = T(0), acc = T(0), comp = T(0);
     const uint32_t nblk = (steps + U - 1) / U;
     for (uint32_t b = 0; b < nblk; ++b)
     {
+#ifndef SBG_ROW_PAD_FULL
+      af = min(af, af_last);
+#endif
       T blk = T(0);
 #pragma unroll
       for (int u = 0; u < U; ++u)
@@ -363,8 +372,14 @@ namespace sbg
           if (SMEM)
           {
             // Row in segment layout plus sentinel padding: at most
-            // steps + U - 1 advances can reach the row side.
+            // steps + U - 1 advances can reach the row side, or, with the
+            // row address pulled back at every block start (VAR 5), U past
+            // the last element.
+#ifndef SBG_ROW_PAD_FULL
+            const uint32_t pad_end = VAR == 5 ? rlen + U : rlen + maxlc + U;
+#else
             const uint32_t pad_end = rlen + maxlc + U;
+#endif
             if (pad_end > L.row_cap) continue;  // host sized row_cap; never expected
             const T* rp = Pp->rpts + 2 * roff;
             const T vlast = rp[2 * (rlen - 1) + 1];
@@ -404,7 +419,7 @@ namespace sbg
             if (VAR == 1) res = merge_pair<T, K, U, 32, false>(rbuf, cols + lane, steps, rlen, p);
             else if (VAR == 5)
               res = merge_smem_soa<T, K, U>(reinterpret_cast<const T*>(rbuf), L.row_cap * (uint32_t)sizeof(T),
-                                            cols + lane, steps, p);
+                                            cols + lane, steps, rlen, p);
             else res = merge_smem_pred<T, K, U>(rbuf, cols + lane, steps, p);
             __syncwarp();
           }

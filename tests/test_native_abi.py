@@ -85,6 +85,27 @@ def test_invalid_pcf_input_rejected_before_device(lib):
     assert b"no breakpoints" in lib.sbg_last_error()
 
 
+def test_large_input_validation_reports_first_invalid_pcf(lib):
+    """Inputs of a million points and more are checked by the host thread
+    pool in parallel ranges; the error still names the first invalid PCF."""
+    h = ctypes.c_void_p()
+    P = lambda a: ctypes.c_void_p(a.ctypes.data)
+    out = np.zeros(1, np.float64)
+    n, L = 3000, 400
+    t = np.tile(np.arange(L, dtype=np.float64), n)
+    pts = np.stack([t, np.ones(n * L)], 1)
+    off = (np.arange(n + 1, dtype=np.uint64) * L).astype(np.uint64)
+    bad = pts.copy()
+    bad[2900 * L + 7, 0] = -1.0
+    bad[1200 * L + 9, 0] = -1.0
+    assert lib.sbg_create_integrate_task(1, 0, 1.0, 1, P(bad), P(off), n, P(out), ctypes.byref(h)) == -2
+    assert b"PCF 1200:" in lib.sbg_last_error() and b"non-decreasing" in lib.sbg_last_error()
+    last = pts.copy()
+    last[(n - 1) * L, 0] = 0.5
+    assert lib.sbg_create_integrate_task(1, 0, 1.0, 1, P(last), P(off), n, P(out), ctypes.byref(h)) == -2
+    assert b"PCF 2999:" in lib.sbg_last_error() and b"t=0" in lib.sbg_last_error()
+
+
 def test_settings_roundtrip(lib):
     import stablebear_gb300 as sb
     sb.set_cuda_threshold(123)
