@@ -692,7 +692,7 @@ def main():
     # What binds the kernel: shared-memory wavefronts.  A warp-step (one
     # rectangle per lane) issues three predicated loads, the row's time and
     # value words (one wavefront each) and the column's 8-byte element (two:
-    # a 64-bit load touches both half-warps); ncu measures 4.2 per warp-step,
+    # a 64-bit load touches both half-warps); ncu measures 4.1 per warp-step,
     # at most one wavefront per SM per clock.
     if mhz:
         ceiling = sms * mhz * 1e6 * 32 / 4.0
