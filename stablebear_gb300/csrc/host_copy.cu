@@ -14,6 +14,7 @@
 #include <functional>
 #include <mutex>
 #include <thread>
+#include <unistd.h>
 #include <vector>
 
 namespace sbg
@@ -21,14 +22,17 @@ namespace sbg
   namespace
   {
     // Fixed pool of host threads.  run() splits one job into parts, one per
-    // thread plus the caller, and returns when every part is done.
+    // thread plus the caller, and returns when every part is done.  The pool
+    // lives until the process ends and is never joined: a child forked after
+    // the threads started has none of them, and joining them there (at exit)
+    // would wait forever.
     class CopyPool
     {
     public:
       static CopyPool& get()
       {
-        static CopyPool pool;
-        return pool;
+        static CopyPool* pool = new CopyPool();
+        return *pool;
       }
 
       unsigned parts() const { return (unsigned)m_threads.size() + 1; }
@@ -36,9 +40,11 @@ namespace sbg
       // job(part) for part in [0, parts()); the caller runs the last part.
       void run(const std::function<void(unsigned)>& job)
       {
-        if (m_threads.empty())
+        if (m_threads.empty() || getpid() != m_pid)
         {
-          job(0);
+          // no pool threads, or a child forked after they started (it has
+          // none of them): every part on the calling thread
+          for (unsigned k = 0; k < parts(); ++k) job(k);
           return;
         }
         std::unique_lock<std::mutex> call(m_call);  // one job at a time
@@ -72,23 +78,12 @@ namespace sbg
       }
 
     private:
-      CopyPool()
+      CopyPool() : m_pid(getpid())
       {
         unsigned hc = std::thread::hardware_concurrency();
         unsigned n = hc > 1 ? std::min(hc, 32u) - 1 : 0;
         for (unsigned i = 0; i < n; ++i) m_threads.emplace_back([this, i] { work(i); });
       }
-      ~CopyPool()
-      {
-        {
-          std::lock_guard<std::mutex> lk(m_mu);
-          m_quit = true;
-          ++m_gen;
-        }
-        m_cv.notify_all();
-        for (auto& t : m_threads) t.join();
-      }
-
       void work(unsigned idx)
       {
         uint64_t seen = 0;
@@ -99,7 +94,6 @@ namespace sbg
             std::unique_lock<std::mutex> lk(m_mu);
             m_cv.wait(lk, [&] { return m_gen != seen; });
             seen = m_gen;
-            if (m_quit) return;
             job = m_job;
           }
           (*job)(idx);
@@ -116,7 +110,7 @@ namespace sbg
       const std::function<void(unsigned)>* m_job = nullptr;
       size_t m_pending = 0;
       uint64_t m_gen = 0;
-      bool m_quit = false;
+      pid_t m_pid;
     };
 
     // Process-wide pinned staging buffers (allocated on first use, reused).

@@ -105,6 +105,26 @@ def test_large_input_validation_reports_first_invalid_pcf(lib):
     assert lib.sbg_create_integrate_task(1, 0, 1.0, 1, P(last), P(off), n, P(out), ctypes.byref(h)) == -2
     assert b"PCF 2999:" in lib.sbg_last_error() and b"t=0" in lib.sbg_last_error()
 
+    # A child forked after the pool's threads started has none of them: the
+    # same check there runs its parts on the calling thread, and the child
+    # exits without waiting for threads it does not have.
+    import multiprocessing as mp
+    q = mp.get_context("fork").Queue()
+
+    def child():
+        st = lib.sbg_create_integrate_task(1, 0, 1.0, 1, P(bad), P(off), n, P(out), ctypes.byref(ctypes.c_void_p()))
+        q.put((st, lib.sbg_last_error()))
+
+    proc = mp.get_context("fork").Process(target=child)
+    proc.start()
+    proc.join(60)
+    alive = proc.is_alive()
+    if alive:
+        proc.kill()
+    assert not alive and proc.exitcode == 0
+    st, msg = q.get(timeout=5)
+    assert st == -2 and b"PCF 1200:" in msg
+
 
 def test_settings_roundtrip(lib):
     import stablebear_gb300 as sb
