@@ -235,14 +235,11 @@ namespace sbg
       SBG_CUDA(cudaMemcpyAsync(dev_dst, host_src, bytes, cudaMemcpyHostToDevice, st));
       return;
     }
-    if (!p.buf[0])
+    // each piece on its own, so a failed allocation leaves nothing half made
+    for (int k = 0; k < 2; ++k)
     {
-      for (int k = 0; k < 2; ++k)
-      {
-        SBG_CUDA(cudaHostAlloc(&p.buf[k], UploadPool::CHUNK, cudaHostAllocDefault));
-        SBG_CUDA(cudaEventCreateWithFlags(&p.ev[k], cudaEventDisableTiming));
-        SBG_CUDA(cudaEventRecord(p.ev[k], st));
-      }
+      if (!p.ev[k]) SBG_CUDA(cudaEventCreateWithFlags(&p.ev[k], cudaEventDisableTiming));
+      if (!p.buf[k]) SBG_CUDA(cudaHostAlloc(&p.buf[k], UploadPool::CHUNK, cudaHostAllocDefault));
     }
     char* dst = static_cast<char*>(dev_dst);
     const char* src = static_cast<const char*>(host_src);
