@@ -274,6 +274,10 @@ void sbg_batch_destroy(sbg_batch* batch);
  * fixed array of SBG_NOALLOC_SCRATCH_BYTES inside the library, which every
  * GPU that loads the library holds until the process exits.
  *   - max_points must be given (measuring it would need scratch of its own).
+ *   - n_row_points / n_col_points must equal row_offsets[n_rows] /
+ *     col_offsets[n_cols] (the host cannot read device offsets without a
+ *     copy).  They size the packed copy; an undercount leaves the entries of
+ *     PCFs past it unwritten while the call still returns SBG_OK.
  *   - A problem whose scratch would exceed SBG_NOALLOC_SCRATCH_BYTES is
  *     rejected with SBG_ERR_INVALID_ARGUMENT and a message giving both sizes;
  *     PCFs that fit the shared-memory kernel need only 256 bytes, whatever n.
@@ -305,6 +309,23 @@ int sbg_length_order_device(const uint64_t* offsets, uint64_t n, uint32_t* perm,
  * and after a region to count the region's launches.  No counterpart in the
  * reference. */
 uint64_t sbg_kernel_launches(void);
+
+/* Host-side fault injection for the out-of-memory path.  Every device
+ * allocation of the library (scratch, packed layouts, output bands) goes
+ * through one allocator; with a limit set, an allocation that would take the
+ * bytes the library holds above it fails before any CUDA call, and the entry
+ * point returns SBG_ERR_OUT_OF_MEMORY with a message naming the sizes, as a
+ * real cudaMalloc failure does.  No device memory is touched, so the next
+ * call (with the limit lifted) runs normally.  SBG_ALLOC_UNLIMITED (the
+ * default) removes the limit; 0 refuses every allocation.  Process-wide.
+ * Replaces the reference's CHK_CUDA failure path
+ * (include/sbear/cuda/cuda_util.cuh:8-10), which has no injection hook. */
+#define SBG_ALLOC_UNLIMITED (~(uint64_t)0)
+int sbg_set_alloc_limit(uint64_t bytes);
+/* Device allocations the library has made in this process so far, and the
+ * bytes it holds now.  No counterpart in the reference. */
+uint64_t sbg_device_allocations(void);
+uint64_t sbg_device_bytes_held(void);
 
 /* Number of output elements of a problem (n(n-1)/2, n(n+1)/2 or n_rows*n_cols). */
 uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols);

@@ -3,10 +3,14 @@
 * ``oracle/liboracle.so`` — the C restatement in ``pcf_oracle.c``; built on
   every machine (gcc, ``-ffp-contract=off`` so x86-64 and aarch64 round the
   same way).
+* ``oracle/liboracle_o3_off.so`` / ``liboracle_o3_fast.so`` — the same source
+  built ``-O3`` for the host CPU without and with FMA contraction; only the
+  CPU-baseline timings use them.
 * ``oracle/_ref/libsbref.so`` — ``ref_harness.cpp`` compiled against the
   stablebear reference's own headers.  Built only when the reference tree is
-  present (``SBREF_ROOT``, default ``/root/reference``); the reference is
-  never copied into this repository.
+  present: ``SBREF_ROOT`` when set, else a stablebear checkout named
+  ``reference`` beside this repository's directory.  The reference is never
+  copied into this repository.
 * ``oracle/_ref/ref_kernels.cubin`` + ``ref_kernels.json`` — the reference's
   own CUDA block kernel (``ref_gpu_kernel.cu`` instantiating
   ``include/sbear/cuda/cuda_pcf_kernel.cuh``), device code only, for sm_103a,
@@ -27,7 +31,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libsbref.so")
-REF_ROOT = os.environ.get("SBREF_ROOT", "/root/reference")
+REF_ROOT = os.environ.get("SBREF_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def _stale(target: str, sources: list[str]) -> bool:
@@ -44,6 +48,32 @@ def build_oracle(force: bool = False) -> str:
                "-o", ORACLE_SO, src, "-lpthread", "-lm"]
         subprocess.run(cmd, check=True)
     return ORACLE_SO
+
+
+# Timed CPU-baseline builds of the same source: optimised for the host CPU,
+# once without and once with FMA contraction (the reference's own builds use
+# gcc defaults, which contract `val += (r - l) * op` into an FMA where the
+# target has one).  The bitwise parity tests keep the -O2 -ffp-contract=off
+# build above; these two only time the CPU path.
+TIMED_SO = {"off": os.path.join(HERE, "liboracle_o3_off.so"), "fast": os.path.join(HERE, "liboracle_o3_fast.so")}
+
+
+def native_cpu_flag() -> str:
+    import platform
+    # gcc spells "tune and select instructions for this CPU" -mcpu on Arm, -march on x86
+    return "-mcpu=native" if platform.machine().lower() in ("aarch64", "arm64") else "-march=native"
+
+
+def build_oracle_timed(contract: str = "fast", force: bool = False) -> str:
+    if contract not in TIMED_SO:
+        raise ValueError("contract must be 'off' or 'fast'")
+    src = os.path.join(HERE, "pcf_oracle.c")
+    out = TIMED_SO[contract]
+    if force or _stale(out, [src, __file__]):
+        cmd = ["gcc", "-O3", native_cpu_flag(), "-std=c11", f"-ffp-contract={contract}", "-fPIC", "-shared",
+               "-o", out, src, "-lpthread", "-lm"]
+        subprocess.run(cmd, check=True)
+    return out
 
 
 def build_ref(force: bool = False) -> str | None:
@@ -120,6 +150,8 @@ def build_ref_gpu_harness(force: bool = False) -> str:
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
+    print(build_oracle_timed("off", force))
+    print(build_oracle_timed("fast", force))
     print(build_ref(force))
     print(build_ref_gpu_kernel(force))
     print(build_ref_gpu_harness(force))

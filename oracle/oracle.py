@@ -26,16 +26,24 @@ from . import build_oracle as _build
 OP_L1, OP_LP, OP_L2 = 0, 1, 2
 MODE_CROSS, MODE_PDIST, MODE_KERNEL = 0, 1, 2
 
-_lib = None
+_libs = {}
 _ref = None
 _P = ctypes.c_void_p
 _U64 = ctypes.c_uint64
 
 
-def _load():
-    global _lib
-    if _lib is None:
-        path = _build.build_oracle()
+def _load(build="check"):
+    """The oracle library: ``"check"`` is the -O2 -ffp-contract=off build every
+    parity test uses; ``"o3_off"`` / ``"o3_fast"`` are the -O3 host-CPU builds
+    without / with FMA contraction that only the CPU-baseline timings use."""
+    lib = _libs.get(build)
+    if lib is None:
+        if build == "check":
+            path = _build.build_oracle()
+        elif build in ("o3_off", "o3_fast"):
+            path = _build.build_oracle_timed(build[3:])
+        else:
+            raise ValueError(f"unknown oracle build {build!r}")
         lib = ctypes.CDLL(path)
         lib.sbo_evaluate.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                      _P, _P, _U64, _P, _P, _U64, _P, ctypes.c_int]
@@ -61,8 +69,10 @@ def _load():
         lib.sbo_lp_norm.restype = ctypes.c_int
         lib.sbo_barcodes_to_pcfs.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, _U64, _P, _P]
         lib.sbo_barcodes_to_pcfs.restype = ctypes.c_int
-        _lib = lib
-    return _lib
+        lib.sbo_evaluate_rows_chunked.argtypes = lib.sbo_evaluate_rows.argtypes + [_U64]
+        lib.sbo_evaluate_rows_chunked.restype = ctypes.c_int
+        _libs[build] = lib
+    return lib
 
 
 def ref_lib():
@@ -158,11 +168,14 @@ def evaluate(points, offsets, *, op=OP_L1, p=1.0, mode=MODE_PDIST, col_points=No
 
 
 def evaluate_rows(points, offsets, rows, *, op=OP_L1, p=1.0, mode=MODE_PDIST, truth=False, threads=None,
-                  col_points=None, col_offsets=None):
+                  col_points=None, col_offsets=None, chunk=0, build="check"):
     """Evaluate only the listed rows.  Returns (values, row_starts) where row
     ``rows[k]``'s results occupy ``values[row_starts[k]:row_starts[k+1]]``
-    (columns 0..i-1 for pdist, 0..i for the kernel, all for cdist)."""
-    lib = _load()
+    (columns 0..i-1 for pdist, 0..i for the kernel, all for cdist).
+    ``chunk`` > 0 hands the threads pieces of at most that many pairs of a
+    row instead of whole rows (no idle threads behind a few long rows);
+    ``build`` picks the library (see ``_load``)."""
+    lib = _load(build)
     points, offsets = _csr(points, offsets)
     dt = _dtype_code(points)
     nr = len(offsets) - 1
@@ -181,9 +194,9 @@ def evaluate_rows(points, offsets, rows, *, op=OP_L1, p=1.0, mode=MODE_PDIST, tr
     if threads is None:
         threads = os.cpu_count() or 1
     base = np.ascontiguousarray(starts[:-1])
-    lib.sbo_evaluate_rows(dt, 1 if truth else 0, op, float(p), mode, _ptr(points), _ptr(offsets), nr,
-                          _ptr(col_points), _ptr(col_offsets), nc, _ptr(rows), len(rows), _ptr(base),
-                          _ptr(out), int(threads))
+    lib.sbo_evaluate_rows_chunked(dt, 1 if truth else 0, op, float(p), mode, _ptr(points), _ptr(offsets), nr,
+                                  _ptr(col_points), _ptr(col_offsets), nc, _ptr(rows), len(rows), _ptr(base),
+                                  _ptr(out), int(threads), int(chunk))
     return out, starts
 
 
@@ -358,7 +371,26 @@ def ref_gpu_triangle(dev_points_ptr, dev_offsets_ptr, n, *, op="l1", p=1.0, kern
     reference scheduler's parameters.  Returns (summed tile-kernel
     milliseconds, tiles).  With host_out (an array of `dtype` and the
     condensed size) the tiles are also scattered into it."""
-    import json
+    _ref_gpu_lib()
+    dtype, entry = _ref_gpu_entry(op, kernel, dtype)
+    ms = ctypes.c_double(0.0)
+    tiles = ctypes.c_uint64(0)
+    err = ctypes.create_string_buffer(512)
+    hp = None
+    if host_out is not None:
+        assert host_out.dtype == dtype and host_out.flags["C_CONTIGUOUS"]
+        assert host_out.size == out_size(MODE_KERNEL if kernel else MODE_PDIST, n)
+        hp = _ptr(host_out)
+    rc = _ref_gpu.sbref_gpu_triangle(_build.REF_CUBIN.encode(), entry.encode(), dtype.itemsize,
+                                     2 if kernel else 1, float(p),
+                                     int(dev_points_ptr), int(dev_offsets_ptr), int(n), hp, int(max_output_elements),
+                                     ctypes.byref(ms), ctypes.byref(tiles), err, len(err))
+    if rc != 0:
+        raise RuntimeError(err.value.decode())
+    return ms.value, int(tiles.value)
+
+
+def _ref_gpu_lib():
     global _ref_gpu
     ok = ref_gpu_kernel_available()
     if ok is not True:
@@ -370,7 +402,17 @@ def ref_gpu_triangle(dev_points_ptr, dev_offsets_ptr, n, *, op="l1", p=1.0, kern
                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
                                            ctypes.c_char_p, ctypes.c_size_t]
         lib.sbref_gpu_triangle.restype = ctypes.c_int
+        lib.sbref_gpu_triangle_rows.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_double, _U64, _U64, _U64, _P, _P, _U64, _P, _U64,
+                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64),
+                                                ctypes.c_char_p, ctypes.c_size_t]
+        lib.sbref_gpu_triangle_rows.restype = ctypes.c_int
         _ref_gpu = lib
+    return _ref_gpu
+
+
+def _ref_gpu_entry(op, kernel, dtype):
+    import json
     with open(_build.REF_ENTRIES) as f:
         entries = json.load(f)
     dtype = np.dtype(dtype)
@@ -379,21 +421,33 @@ def ref_gpu_triangle(dev_points_ptr, dev_offsets_ptr, n, *, op="l1", p=1.0, kern
     key = ("inner" if kernel else op) + ("_f32" if dtype == np.float32 else "_f64")
     if key not in entries:
         raise ValueError(f"no reference kernel for {key}")
+    return dtype, entries[key]
+
+
+def ref_gpu_triangle_rows(dev_points_ptr, dev_offsets_ptr, n, rows, *, op="l1", p=1.0, kernel=False,
+                          dtype=np.float32, max_output_elements=0):
+    """As ref_gpu_triangle, copying back only the listed rows of the
+    triangle.  Returns (summed tile-kernel milliseconds, tiles, values,
+    row_starts) with row ``rows[k]``'s entries (columns 0..i-1 for pdist,
+    0..i for the kernel) at ``values[row_starts[k]:row_starts[k+1]]``."""
+    lib = _ref_gpu_lib()
+    dtype, entry = _ref_gpu_entry(op, kernel, dtype)
+    rows = np.ascontiguousarray(rows, dtype=np.uint64)
+    counts = rows + (1 if kernel else 0)
+    starts = np.zeros(len(rows) + 1, dtype=np.uint64)
+    np.cumsum(counts, out=starts[1:])
+    vals = np.full(int(starts[-1]), np.nan, dtype=dtype)
+    base = np.ascontiguousarray(starts[:-1])
     ms = ctypes.c_double(0.0)
     tiles = ctypes.c_uint64(0)
     err = ctypes.create_string_buffer(512)
-    hp = None
-    if host_out is not None:
-        assert host_out.dtype == dtype and host_out.flags["C_CONTIGUOUS"]
-        assert host_out.size == out_size(MODE_KERNEL if kernel else MODE_PDIST, n)
-        hp = _ptr(host_out)
-    rc = _ref_gpu.sbref_gpu_triangle(_build.REF_CUBIN.encode(), entries[key].encode(), dtype.itemsize,
-                                     2 if kernel else 1, float(p),
-                                     int(dev_points_ptr), int(dev_offsets_ptr), int(n), hp, int(max_output_elements),
-                                     ctypes.byref(ms), ctypes.byref(tiles), err, len(err))
+    rc = lib.sbref_gpu_triangle_rows(_build.REF_CUBIN.encode(), entry.encode(), dtype.itemsize, 2 if kernel else 1,
+                                     float(p), int(dev_points_ptr), int(dev_offsets_ptr), int(n), _ptr(rows),
+                                     _ptr(base), len(rows), _ptr(vals), int(max_output_elements), ctypes.byref(ms),
+                                     ctypes.byref(tiles), err, len(err))
     if rc != 0:
         raise RuntimeError(err.value.decode())
-    return ms.value, int(tiles.value)
+    return ms.value, int(tiles.value), vals, starts
 
 
 def rectangles(f, g, a=0.0, b=float("inf")):

@@ -251,6 +251,9 @@ typedef struct {
   void* out;
   int compact;           /* 1: write each evaluated row's results back to back */
   const uint64_t* compact_base; /* per listed row: first output slot when compact */
+  uint64_t chunk;        /* > 0: work items are pieces of at most `chunk` pairs of a row */
+  const uint64_t* chunk_first; /* per listed row: its first work item (nrows + 1 entries) */
+  uint64_t nitems;       /* work items handed out */
   _Atomic uint64_t next;
 } sbo_job;
 
@@ -261,13 +264,19 @@ static inline uint64_t sbo_cond_index(int mode, uint64_t i, uint64_t j)
   return r * (r + 1) / 2 + c;                /* symmetric_matrix.hpp:257-259 */
 }
 
-static void sbo_eval_row(sbo_job* job, uint64_t k)
+static uint64_t sbo_row_len(const sbo_job* job, uint64_t i)
+{
+  if (job->mode == 1) return i;
+  if (job->mode == 2) return i + 1;
+  return job->nc;
+}
+
+/* Pairs (i, j) of listed row k for j in [jlo, jhi). */
+static void sbo_eval_range(sbo_job* job, uint64_t k, uint64_t jlo, uint64_t jhi)
 {
   uint64_t i = job->rows ? job->rows[k] : k;
-  uint64_t jbeg = 0, jend = job->nc;
-  if (job->mode == 1) jend = i;
-  else if (job->mode == 2) jend = i + 1;
-  for (uint64_t j = jbeg; j < jend; ++j) {
+  const uint64_t jbeg = 0;
+  for (uint64_t j = jlo; j < jhi; ++j) {
     uint64_t slot;
     if (job->compact) slot = job->compact_base[k] + (j - jbeg);
     else if (job->mode == 0) slot = i * job->nc + j;
@@ -296,13 +305,33 @@ static void sbo_eval_row(sbo_job* job, uint64_t k)
   }
 }
 
+static void sbo_eval_item(sbo_job* job, uint64_t u)
+{
+  if (job->chunk == 0) {
+    uint64_t i = job->rows ? job->rows[u] : u;
+    sbo_eval_range(job, u, 0, sbo_row_len(job, i));
+    return;
+  }
+  /* the listed row holding item u: last k with chunk_first[k] <= u */
+  uint64_t lo = 0, hi = job->nrows - 1;
+  while (lo < hi) {
+    uint64_t mid = (lo + hi + 1) / 2;
+    if (job->chunk_first[mid] <= u) lo = mid; else hi = mid - 1;
+  }
+  uint64_t i = job->rows ? job->rows[lo] : lo;
+  uint64_t len = sbo_row_len(job, i);
+  uint64_t jlo = (u - job->chunk_first[lo]) * job->chunk;
+  uint64_t jhi = jlo + job->chunk < len ? jlo + job->chunk : len;
+  sbo_eval_range(job, lo, jlo, jhi);
+}
+
 static void* sbo_worker(void* arg)
 {
   sbo_job* job = (sbo_job*)arg;
   for (;;) {
-    uint64_t k = atomic_fetch_add(&job->next, 1);
-    if (k >= job->nrows) break;
-    sbo_eval_row(job, k);
+    uint64_t u = atomic_fetch_add(&job->next, 1);
+    if (u >= job->nitems) break;
+    sbo_eval_item(job, u);
   }
   return NULL;
 }
@@ -336,7 +365,7 @@ int sbo_evaluate(int dtype, int kind, int op, double p, int mode,
   job.rpts = rpts; job.roff = roff; job.nr = nr;
   if (mode != 0) { cpts = rpts; coff = roff; nc = nr; }
   job.cpts = cpts; job.coff = coff; job.nc = nc;
-  job.rows = NULL; job.nrows = nr; job.out = out;
+  job.rows = NULL; job.nrows = nr; job.nitems = nr; job.out = out;
   return sbo_run(&job, nthreads);
 }
 
@@ -355,9 +384,42 @@ int sbo_evaluate_rows(int dtype, int kind, int op, double p, int mode,
   job.rpts = rpts; job.roff = roff; job.nr = nr;
   if (mode != 0) { cpts = rpts; coff = roff; nc = nr; }
   job.cpts = cpts; job.coff = coff; job.nc = nc;
-  job.rows = rows; job.nrows = nrows; job.out = out;
+  job.rows = rows; job.nrows = nrows; job.nitems = nrows; job.out = out;
   job.compact = 1; job.compact_base = compact_base;
   return sbo_run(&job, nthreads);
+}
+
+/* As sbo_evaluate_rows, with the threads taking pieces of at most `chunk`
+ * pairs of a row instead of whole rows, so that a few long rows cannot leave
+ * threads idle at the end (row i of a pdist has i pairs). */
+int sbo_evaluate_rows_chunked(int dtype, int kind, int op, double p, int mode,
+                              const void* rpts, const uint64_t* roff, uint64_t nr,
+                              const void* cpts, const uint64_t* coff, uint64_t nc,
+                              const uint64_t* rows, uint64_t nrows, const uint64_t* compact_base,
+                              void* out, int nthreads, uint64_t chunk)
+{
+  if (chunk == 0 || nrows == 0)
+    return sbo_evaluate_rows(dtype, kind, op, p, mode, rpts, roff, nr, cpts, coff, nc, rows, nrows, compact_base,
+                             out, nthreads);
+  sbo_job job;
+  memset(&job, 0, sizeof(job));
+  job.dtype = dtype; job.kind = kind; job.op = op; job.p = p; job.mode = mode;
+  job.rpts = rpts; job.roff = roff; job.nr = nr;
+  if (mode != 0) { cpts = rpts; coff = roff; nc = nr; }
+  job.cpts = cpts; job.coff = coff; job.nc = nc;
+  job.rows = rows; job.nrows = nrows; job.out = out;
+  job.compact = 1; job.compact_base = compact_base;
+  uint64_t* first = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)(nrows + 1));
+  if (!first) return -1;
+  first[0] = 0;
+  for (uint64_t k = 0; k < nrows; ++k) {
+    uint64_t len = sbo_row_len(&job, rows[k]);
+    first[k + 1] = first[k] + (len + chunk - 1) / chunk;
+  }
+  job.chunk = chunk; job.chunk_first = first; job.nitems = first[nrows];
+  int rc = sbo_run(&job, nthreads);
+  free(first);
+  return rc;
 }
 
 /* Total merged rectangles (segments) of a pairwise/cross problem, the work

@@ -17,7 +17,8 @@
 // each tile's rows and columns), and the timed region holds the tile
 // kernels only: no per-tile clearing, no copies, no host scatter.  That is
 // the reference kernel's best case.  With a host output the tiles are
-// copied back and scattered into condensed storage (parity checks).
+// copied back and scattered into condensed storage (parity checks); with a
+// row sample only the sampled rows of each tile are copied back.
 //
 // The kernel is reached through the CUDA driver API (cuModuleLoad,
 // cuLaunchKernel) with the parameter block of PcfBlockKernelParams<T, T>
@@ -69,10 +70,21 @@ namespace
 
 namespace
 {
+  // Sampled rows to copy back instead of the whole triangle: row srows[k]'s
+  // entries j (j < i for pdist, j <= i for the kernel) land at sout[sbase[k] + j].
+  template <typename T>
+  struct RowSample
+  {
+    const uint64_t* rows = nullptr;
+    const uint64_t* base = nullptr;
+    uint64_t count = 0;
+    T* out = nullptr;
+  };
+
   template <typename T>
   int run_triangle(const char* cubin, const char* entry, int skip_mode, double p, uint64_t dpts, uint64_t doff,
                    uint64_t n, T* host_out, uint64_t max_output_elements, double* kernel_ms, uint64_t* n_tiles,
-                   char* err, size_t errlen)
+                   char* err, size_t errlen, const RowSample<T>& sample = RowSample<T>())
 {
   CUmodule mod = nullptr;
   CUdeviceptr tile = 0;
@@ -108,6 +120,7 @@ namespace
     if (cap == 0) { if (kernel_ms) *kernel_ms = 0; cuModuleUnload(mod); return 0; }
     check(cuMemAlloc(&tile, cap * sizeof(T)), "tile buffer");
     if (host_out) htile.resize(cap);
+    else if (sample.count) htile.resize(sched.max_col_width());
     check(cuEventCreate(&e0, CU_EVENT_DEFAULT), "event");
     check(cuEventCreate(&e1, CU_EVENT_DEFAULT), "event");
 
@@ -156,6 +169,23 @@ namespace
           }
         }
       }
+      else if (sample.count)
+      {
+        for (uint64_t k = 0; k < sample.count; ++k)
+        {
+          const uint64_t i = sample.rows[k];
+          if (i < blk.rowStart || i >= blk.rowStart + blk.rowHeight) continue;
+          const uint64_t il = i - blk.rowStart;
+          check(cuMemcpyDtoH(htile.data(), tile + il * blk.colWidth * sizeof(T), blk.colWidth * sizeof(T)),
+                "row copy");
+          for (size_t jl = 0; jl < blk.colWidth; ++jl)
+          {
+            const uint64_t j = blk.colStart + jl;
+            if (skip_mode == 1 ? j >= i : j > i) continue;
+            sample.out[sample.base[k] + j] = htile[jl];
+          }
+        }
+      }
     }
     if (kernel_ms) *kernel_ms = total_ms;
     cuEventDestroy(e0);
@@ -188,6 +218,31 @@ extern "C" int sbref_gpu_triangle(const char* cubin, const char* entry, int elem
   if (elem_bytes == 8)
     return run_triangle<double>(cubin, entry, skip_mode, p, dpts, doff, n, static_cast<double*>(host_out),
                                 max_output_elements, kernel_ms, n_tiles, err, errlen);
+  if (err && errlen) std::snprintf(err, errlen, "elem_bytes must be 4 or 8");
+  return -1;
+}
+
+// As sbref_gpu_triangle, copying back only the listed rows (a few rows of a
+// 20 GB triangle instead of a host scatter of all of it): row rows[k]'s
+// entries j land at sample_out[row_base[k] + j].
+extern "C" int sbref_gpu_triangle_rows(const char* cubin, const char* entry, int elem_bytes, int skip_mode, double p,
+                                       uint64_t dpts, uint64_t doff, uint64_t n, const uint64_t* rows,
+                                       const uint64_t* row_base, uint64_t n_rows, void* sample_out,
+                                       uint64_t max_output_elements, double* kernel_ms, uint64_t* n_tiles, char* err,
+                                       size_t errlen)
+{
+  if (elem_bytes == 4)
+  {
+    RowSample<float> s{rows, row_base, n_rows, static_cast<float*>(sample_out)};
+    return run_triangle<float>(cubin, entry, skip_mode, p, dpts, doff, n, nullptr, max_output_elements, kernel_ms,
+                               n_tiles, err, errlen, s);
+  }
+  if (elem_bytes == 8)
+  {
+    RowSample<double> s{rows, row_base, n_rows, static_cast<double*>(sample_out)};
+    return run_triangle<double>(cubin, entry, skip_mode, p, dpts, doff, n, nullptr, max_output_elements, kernel_ms,
+                                n_tiles, err, errlen, s);
+  }
   if (err && errlen) std::snprintf(err, errlen, "elem_bytes must be 4 or 8");
   return -1;
 }

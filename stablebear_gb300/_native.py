@@ -14,6 +14,9 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libsbgpu.so")
 
 SBG_OK = 0
+SBG_ERR_OUT_OF_MEMORY = -4
+SBG_ERR_CANCELLED = -5
+ALLOC_UNLIMITED = (1 << 64) - 1  # SBG_ALLOC_UNLIMITED: no limit on the library's device allocations
 STATUS_NAMES = {
     -1: "SBG_ERR_INVALID_ARGUMENT",
     -2: "SBG_ERR_INVALID_INPUT",
@@ -80,6 +83,9 @@ SIGNATURES = {
     "sbg_batch_destroy": (None, [_P]),
     "sbg_output_count": (_U64, [_I, _U64, _U64]),
     "sbg_kernel_launches": (_U64, []),
+    "sbg_set_alloc_limit": (_I, [_U64]),
+    "sbg_device_allocations": (_U64, []),
+    "sbg_device_bytes_held": (_U64, []),
     "sbg_block_device": (_I, [_I, _I, _D, _I, _P, _P, _P, _P, _U64, _U64, _U64, _U64, ctypes.c_uint32, _P, _P]),
     "sbg_length_order_device": (_I, [_P, _U64, _P, _P]),
     "sbg_measure_peak": (_I, [_I, ctypes.POINTER(_D)]),

@@ -340,19 +340,14 @@ namespace sbg
     SBG_CUDA(cudaMemsetAsync(grad, 0, sizeof(T) * 2 * npts, st));
     if (n == 0) return;
 
-    void* packed = nullptr;
-    void* queue = nullptr;
-    void* paired = nullptr;
-    void* order = nullptr;
-    SBG_CUDA(cudaMallocAsync(&packed, std::max<uint64_t>(1, npts) * sizeof(Elem<T>), st));
-    SBG_CUDA(cudaMallocAsync(&queue, 256, st));
-    SBG_CUDA(cudaMallocAsync(&paired, std::max<uint64_t>(1, npts) * 2 * sizeof(T), st));
-    SBG_CUDA(cudaMallocAsync(&order, n * sizeof(uint32_t), st));
-    struct Free
-    {
-      void* a; void* b; void* c; void* d; cudaStream_t s;
-      ~Free() { cudaFreeAsync(a, s); cudaFreeAsync(b, s); cudaFreeAsync(c, s); cudaFreeAsync(d, s); }
-    } guard{packed, queue, paired, order, st};
+    StreamBuffer packed_buf(std::max<uint64_t>(1, npts) * sizeof(Elem<T>), st);
+    StreamBuffer queue_buf(256, st);
+    StreamBuffer paired_buf(std::max<uint64_t>(1, npts) * 2 * sizeof(T), st);
+    StreamBuffer order_buf(n * sizeof(uint32_t), st);
+    void* packed = packed_buf.get();
+    void* queue = queue_buf.get();
+    void* paired = paired_buf.get();
+    void* order = order_buf.get();
     // The forward's processing order (windows of 1024 PCFs by length): the
     // 32 columns of a group then have similar lengths, so the warp-uniform
     // step count wastes little.  Gradients land at the PCFs' own offsets.

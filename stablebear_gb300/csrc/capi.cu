@@ -261,6 +261,14 @@ extern "C"
 
   uint64_t sbg_kernel_launches(void) { return kernel_launches(); }
 
+  int sbg_set_alloc_limit(uint64_t bytes)
+  {
+    set_alloc_limit(bytes);
+    return SBG_OK;
+  }
+  uint64_t sbg_device_allocations(void) { return device_allocations(); }
+  uint64_t sbg_device_bytes_held(void) { return device_bytes_held(); }
+
   uint64_t sbg_output_count(int skip_mode, uint64_t n_rows, uint64_t n_cols)
   {
     return output_count(skip_mode, n_rows, n_cols);

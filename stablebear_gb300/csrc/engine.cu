@@ -61,12 +61,77 @@ namespace sbg
     return s;
   }
 
+  // ---- device allocations ----------------------------------------------------
+
+  static std::atomic<uint64_t> g_alloc_limit{~0ull};
+  static std::atomic<uint64_t> g_alloc_held{0};
+  static std::atomic<uint64_t> g_alloc_count{0};
+
+  static void reserve_bytes(size_t bytes)
+  {
+    const uint64_t held = g_alloc_held.fetch_add(bytes, std::memory_order_relaxed) + bytes;
+    const uint64_t limit = g_alloc_limit.load(std::memory_order_relaxed);
+    if (held > limit || held < bytes)
+    {
+      g_alloc_held.fetch_sub(bytes, std::memory_order_relaxed);
+      throw Error(ST_OUT_OF_MEMORY, "device allocation of " + std::to_string(bytes) + " bytes refused: " +
+                                        std::to_string(held - bytes) + " bytes held, limit " +
+                                        std::to_string(limit) + " (sbg_set_alloc_limit)");
+    }
+  }
+
+  void* device_malloc(size_t bytes)
+  {
+    reserve_bytes(bytes);
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess)
+    {
+      g_alloc_held.fetch_sub(bytes, std::memory_order_relaxed);
+      throw_cuda(e, __FILE__, __LINE__);
+    }
+    g_alloc_count.fetch_add(1, std::memory_order_relaxed);
+    return p;
+  }
+
+  void device_free(void* p, size_t bytes) noexcept
+  {
+    if (!p) return;
+    cudaFree(p);
+    g_alloc_held.fetch_sub(bytes, std::memory_order_relaxed);
+  }
+
+  void* device_malloc_async(size_t bytes, cudaStream_t st)
+  {
+    reserve_bytes(bytes);
+    void* p = nullptr;
+    const cudaError_t e = cudaMallocAsync(&p, bytes, st);
+    if (e != cudaSuccess)
+    {
+      g_alloc_held.fetch_sub(bytes, std::memory_order_relaxed);
+      throw_cuda(e, __FILE__, __LINE__);
+    }
+    g_alloc_count.fetch_add(1, std::memory_order_relaxed);
+    return p;
+  }
+
+  void device_free_async(void* p, size_t bytes, cudaStream_t st) noexcept
+  {
+    if (!p) return;
+    cudaFreeAsync(p, st);
+    g_alloc_held.fetch_sub(bytes, std::memory_order_relaxed);
+  }
+
+  void set_alloc_limit(uint64_t bytes) { g_alloc_limit.store(bytes, std::memory_order_relaxed); }
+  uint64_t device_allocations() { return g_alloc_count.load(std::memory_order_relaxed); }
+  uint64_t device_bytes_held() { return g_alloc_held.load(std::memory_order_relaxed); }
+
   void DeviceBuffer::reset(size_t bytes)
   {
     release();
     if (bytes)
     {
-      SBG_CUDA(cudaMalloc(&m_ptr, bytes));
+      m_ptr = device_malloc(bytes);
       m_bytes = bytes;
     }
   }
@@ -75,7 +140,7 @@ namespace sbg
   {
     if (m_ptr)
     {
-      cudaFree(m_ptr);
+      device_free(m_ptr, m_bytes);
       m_ptr = nullptr;
       m_bytes = 0;
     }
@@ -415,14 +480,15 @@ namespace sbg
     struct AsyncBuf
     {
       void* p = nullptr;
+      size_t n = 0;
       cudaStream_t s = nullptr;
-      AsyncBuf(size_t bytes, cudaStream_t st) : s(st)
+      AsyncBuf(size_t bytes, cudaStream_t st) : n(bytes), s(st)
       {
-        if (bytes) SBG_CUDA(cudaMallocAsync(&p, bytes, st));
+        if (bytes) p = device_malloc_async(bytes, st);
       }
       ~AsyncBuf()
       {
-        if (p) cudaFreeAsync(p, s);
+        if (p) device_free_async(p, n, s);
       }
       AsyncBuf(const AsyncBuf&) = delete;
       AsyncBuf& operator=(const AsyncBuf&) = delete;

@@ -210,7 +210,9 @@ namespace sbg
 
   namespace
   {
-    // Two pinned buffers for uploads, allocated on first use and reused.
+    // Two pinned buffers and two events for uploads, allocated on first use
+    // and reused; one pool per device, because an event can only be recorded
+    // on a stream of the device it was created on.
     struct UploadPool
     {
       static constexpr size_t CHUNK = 32u << 20;
@@ -218,16 +220,24 @@ namespace sbg
       void* buf[2] = {nullptr, nullptr};
       cudaEvent_t ev[2] = {nullptr, nullptr};
     };
-    UploadPool& upload_pool()
+    constexpr int kUploadDevices = 64;
+    UploadPool& upload_pool(int dev)
     {
-      static UploadPool p;
-      return p;
+      static UploadPool pools[kUploadDevices];
+      return pools[dev];
     }
   }
 
   void upload_pageable(void* dev_dst, const void* host_src, size_t bytes, cudaStream_t st)
   {
-    UploadPool& p = upload_pool();
+    int dev = 0;
+    SBG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kUploadDevices)
+    {
+      SBG_CUDA(cudaMemcpyAsync(dev_dst, host_src, bytes, cudaMemcpyHostToDevice, st));
+      return;
+    }
+    UploadPool& p = upload_pool(dev);
     std::unique_lock<std::mutex> lk(p.mu, std::try_to_lock);
     if (bytes < (16u << 20) || !lk.owns_lock())
     {

@@ -13,6 +13,8 @@
 #include "../../include/sbgpu.h"
 #include "sbg_internal.hpp"
 
+#include <cuda.h>  // CUcontext / CUresult types; the two driver calls are looked up through the runtime
+
 #include <mutex>
 
 namespace sbg
@@ -27,29 +29,70 @@ namespace sbg
 
     constexpr int kMaxDevices = 64;
     std::mutex g_setup_mu;
-    void* g_scratch_addr[kMaxDevices] = {};
+    struct ScratchAddr
+    {
+      void* ptr = nullptr;
+      unsigned long long context = 0;  // id of the CUDA context the address belongs to
+    };
+    ScratchAddr g_scratch_addr[kMaxDevices];
 
-    // Device address of g_noalloc_scratch on the current device.  Host code
-    // only has a stand-in for the array, so the address is looked up once per
-    // device, with that device current, and cached.
+    using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+    using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+    // Unique id of the calling thread's current CUDA context (cuCtxGetId), 0
+    // when none is current yet.  A device reset makes a new context with a
+    // new id, and the library module (with the array) is loaded anew in it.
+    unsigned long long current_context_id()
+    {
+      static CtxGetCurrentFn get_current = nullptr;
+      static CtxGetIdFn get_id = nullptr;
+      static std::once_flag once;
+      std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+          get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+        fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+          get_id = reinterpret_cast<CtxGetIdFn>(fn);
+        cudaGetLastError();
+      });
+      if (!get_current || !get_id) throw Error(ST_CUDA, "cuCtxGetCurrent / cuCtxGetId not available from the driver");
+      CUcontext ctx = nullptr;
+      if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+      unsigned long long id = 0;
+      if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+      return id;
+    }
+
+    // Device address of g_noalloc_scratch in the current device's context.
+    // Host code only has a stand-in for the array, so the address is looked
+    // up with cudaGetSymbolAddress, with the device current, the first time a
+    // context is seen (once per device, again after a device reset), and
+    // cached under the context's id.
     void* scratch_for_current_device()
     {
       int dev = 0;
       SBG_CUDA(cudaGetDevice(&dev));
       if (dev < 0 || dev >= kMaxDevices) throw Error(ST_INVALID_ARGUMENT, "device index out of range");
       std::lock_guard<std::mutex> lock(g_setup_mu);
-      if (!g_scratch_addr[dev])
+      ScratchAddr& s = g_scratch_addr[dev];
+      const unsigned long long ctx = current_context_id();
+      if (!s.ptr || ctx == 0 || ctx != s.context)
       {
         void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // also makes the primary context current
         if (e != cudaSuccess || !p)
         {
           cudaGetLastError();
           throw Error(ST_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch) failed: ") + cudaGetErrorString(e));
         }
-        g_scratch_addr[dev] = p;
+        s.ptr = p;
+        s.context = current_context_id();
       }
-      return g_scratch_addr[dev];
+      return s.ptr;
     }
   }
 }

@@ -1,7 +1,8 @@
-// Issue-rate probes for the roofline denominators: sustained FP32 FFMA and
+// Issue-rate probes reported beside the roofline: sustained FP32 FFMA and
 // FP64 DFMA lane-operations per second on the current device.  Each thread
-// runs 8 independent FMA chains (enough ILP to keep the pipe full); one FMA
-// instruction per lane counts as one lane-op.
+// runs 8 independent FMA chains (enough ILP to keep the pipe full), unrolled
+// 16 times so the loop's own instructions are under 2 % of those issued;
+// one FMA instruction per lane counts as one lane-op.
 #include "../../include/sbgpu.h"
 #include "sbg_internal.hpp"
 
@@ -13,7 +14,7 @@ namespace sbg
     T a0 = seed + T(threadIdx.x), a1 = a0 + T(1), a2 = a0 + T(2), a3 = a0 + T(3);
     T a4 = a0 + T(4), a5 = a0 + T(5), a6 = a0 + T(6), a7 = a0 + T(7);
     const T m = T(0.999999), c = T(1e-7);
-#pragma unroll 4
+#pragma unroll 16
     for (int i = 0; i < ITERS; ++i)
     {
       a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
@@ -36,7 +37,7 @@ namespace sbg
     SBG_CUDA(launched());
     count_launches(1);
     SBG_CUDA(cudaEventRecord(e0));
-    const int reps = 5;
+    const int reps = 20;
     for (int r = 0; r < reps; ++r) fma_rate_kernel<T, ITERS><<<blocks, 256>>>(T(1), sink.as<T>());
     SBG_CUDA(launched());
     count_launches(reps - 1);

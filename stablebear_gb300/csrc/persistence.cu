@@ -343,10 +343,9 @@ namespace sbg
 
     struct AsyncMem
     {
-      void* p = nullptr;
-      cudaStream_t s;
-      AsyncMem(size_t bytes, cudaStream_t st) : s(st) { if (bytes) SBG_CUDA(cudaMallocAsync(&p, bytes, st)); }
-      ~AsyncMem() { if (p) cudaFreeAsync(p, s); }
+      StreamBuffer buf;
+      void* p;
+      AsyncMem(size_t bytes, cudaStream_t st) : buf(bytes, st), p(buf.get()) { }
     };
 
     template <typename T, int KIND>

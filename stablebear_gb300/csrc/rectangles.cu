@@ -199,12 +199,10 @@ namespace sbg
 
     struct DevMem
     {
-      void* p = nullptr;
-      explicit DevMem(size_t bytes) { if (bytes) SBG_CUDA(cudaMalloc(&p, bytes)); }
-      ~DevMem() { if (p) cudaFree(p); }
-      DevMem(const DevMem&) = delete;
-      DevMem& operator=(const DevMem&) = delete;
-      template <typename U> U* as() const { return static_cast<U*>(p); }
+      DeviceBuffer buf;
+      void* p;
+      explicit DevMem(size_t bytes) : buf(bytes), p(buf.get()) { }
+      template <typename U> U* as() const { return buf.as<U>(); }
     };
 
     template <typename T>

@@ -229,4 +229,39 @@ namespace sbg
   void count_launches(uint64_t n);
   void uncount_launches(uint64_t n);
   uint64_t kernel_launches();
+
+  // Every device allocation of the library goes through these four calls
+  // (no other file calls cudaMalloc / cudaMallocAsync / cudaFree /
+  // cudaFreeAsync).  They count allocations and the bytes they hold, and
+  // refuse, with ST_OUT_OF_MEMORY and before any CUDA call, an allocation
+  // that would take the bytes held above the limit set by
+  // sbg_set_alloc_limit: host-side fault injection of the reference's
+  // CHK_CUDA out-of-memory failure (include/sbear/cuda/cuda_util.cuh:8-10).
+  void* device_malloc(size_t bytes);
+  void device_free(void* p, size_t bytes) noexcept;
+  void* device_malloc_async(size_t bytes, cudaStream_t st);
+  void device_free_async(void* p, size_t bytes, cudaStream_t st) noexcept;
+  void set_alloc_limit(uint64_t bytes);
+  uint64_t device_allocations();
+  uint64_t device_bytes_held();
+
+  // RAII stream-ordered device buffer (device_malloc_async / device_free_async).
+  class StreamBuffer
+  {
+  public:
+    StreamBuffer(size_t bytes, cudaStream_t st) : m_bytes(bytes), m_stream(st)
+    {
+      if (bytes) m_ptr = device_malloc_async(bytes, st);
+    }
+    ~StreamBuffer() { device_free_async(m_ptr, m_bytes, m_stream); }
+    StreamBuffer(const StreamBuffer&) = delete;
+    StreamBuffer& operator=(const StreamBuffer&) = delete;
+    void* get() const { return m_ptr; }
+    template <typename U> U* as() const { return static_cast<U*>(m_ptr); }
+
+  private:
+    void* m_ptr = nullptr;
+    size_t m_bytes = 0;
+    cudaStream_t m_stream = nullptr;
+  };
 }

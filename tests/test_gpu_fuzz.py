@@ -8,8 +8,9 @@ memory, hybrid, time-windowed with caps down to one element), a warp count
 and a row chunk.  Every combination must give the same integrals: float32
 within 3e-5 relative of the truth (window caps below 32 only with PCFs of at
 most 150 elements, where the float32 sum they make close to a naive one stays
-inside that), Lp with general p 1e-4; float64 within 1e-11; the L2 kernel
-against max(|truth|, 1).
+inside that), Lp with general p 1e-4; float64 within 1e-12 (general p:
+1e-10, the reference's own GPU-vs-CPU bound for pow in double); the L2
+kernel against max(|truth|, 1).
 """
 import numpy as np
 import pytest
@@ -105,7 +106,7 @@ def test_random_cases_against_truth():
                 raise
             ran += 1
             if dt == np.float64:
-                tol = 1e-11 if tol < 1e-4 else 1e-10
+                tol = 1e-12 if tol < 1e-4 else 1e-10
             err = _rel(got, want, floor)
             if not err <= tol:
                 failures.append((case, dt.__name__, n, variant, cap, warps, chunk, int(what), err))

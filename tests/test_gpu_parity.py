@@ -296,19 +296,89 @@ def test_task_progress_and_stop():
     assert task.work_completed() == task.work_total() == 2000 * 1999 // 2
     assert task.work_step_unit() == "integral"
     task.close()
-    # a stop request either lands before the last band or the task completes
+
+
+def test_task_stop_cancels():
+    """A stop requested right after start is honoured between bands: the
+    worker returns SBG_ERR_CANCELLED (InterruptedError in Python), once, and
+    the task reports less work completed than its total
+    (include/sbear/task.hpp:21-31, rethrown once by wait_for at :84-96).
+    With 256 KB bands the N = 6000 triangle (72 MB) has about 280 bands, each a
+    kernel launch plus a synchronised copy, so the worker cannot finish them
+    all before the stop request a few microseconds after start."""
+    import stablebear_gb300 as sb
+    from stablebear_gb300 import synthetic
+    from stablebear_gb300.distance import Distance_f32_f32
+    pts, off = synthetic.plain_l1(6000, seed=2)
+    X = arr(pts, off)
     sb.set_tuning(band_bytes=256 << 10)
     try:
         task, dm = Distance_f32_f32.pdist_l1(X)
         task.request_stop()
-        try:
+        with pytest.raises(InterruptedError, match="cancelled"):
             task.wait()
-        except InterruptedError:
-            pass
         assert task.stop_requested()
+        assert 0 < task.work_completed() < task.work_total() == 6000 * 5999 // 2
+        task.wait()  # the error surfaces once
         task.close()
+        # the next task runs to completion and matches an uncancelled run
+        task, dm = Distance_f32_f32.pdist_l1(X[:300])
+        task.wait()
+        task.close()
+        np.testing.assert_array_equal(dm.data, sb.pdist(X[:300]).data)
     finally:
         sb.set_tuning()
+
+
+def test_alloc_limit_injects_out_of_memory():
+    """Host-side fault injection of the allocation failure (the reference's
+    CHK_CUDA path, include/sbear/cuda/cuda_util.cuh:8-10): with a limit below
+    what a call needs, the call fails with SBG_ERR_OUT_OF_MEMORY
+    (MemoryError) before it touches device memory, on the device entry, the
+    blocking host entry and a task (whose worker error surfaces from wait);
+    with the limit lifted the same calls succeed."""
+    import ctypes
+    import torch
+    import stablebear_gb300 as sb
+    from stablebear_gb300 import _native as nat, synthetic
+    from stablebear_gb300.distance import Distance_f32_f32
+    lib = nat.lib()
+    pts, off = synthetic.plain_l1(500, seed=9)
+    n = 500
+    want = sb.pdist(arr(pts, off)).data
+    dp = torch.from_numpy(pts).cuda()
+    do = torch.from_numpy(off.astype(np.int64)).cuda()
+    out = torch.full((n * (n - 1) // 2,), -1.0, device="cuda")
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def device_call():
+        return lib.sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_LOWER_NODIAG, dp.data_ptr(), do.data_ptr(),
+                                       n, None, None, 0, None, None, 0, out.data_ptr(), 0, 0, 0, st)
+
+    held = lib.sbg_device_bytes_held()
+    try:
+        assert lib.sbg_set_alloc_limit(0) == 0
+        allocs = lib.sbg_device_allocations()
+        assert device_call() == nat.SBG_ERR_OUT_OF_MEMORY
+        assert "sbg_set_alloc_limit" in nat.last_error()
+        torch.cuda.synchronize()
+        assert bool((out == -1.0).all())                      # nothing ran
+        with pytest.raises(MemoryError, match="refused"):
+            sb.pdist(arr(pts, off))                          # blocking host entry
+        task, dm = Distance_f32_f32.pdist_l1(arr(pts, off))  # task: the worker's error, once
+        with pytest.raises(MemoryError):
+            task.wait()
+        task.wait()
+        task.close()
+        assert lib.sbg_device_allocations() == allocs
+        assert lib.sbg_device_bytes_held() == held
+    finally:
+        lib.sbg_set_alloc_limit(nat.ALLOC_UNLIMITED)
+    assert device_call() == 0
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy(), want)
+    np.testing.assert_array_equal(sb.pdist(arr(pts, off)).data, want)
+    assert lib.sbg_device_bytes_held() == held
 
 
 def test_invalid_input_raises_value_error():

@@ -56,6 +56,25 @@ def test_reference_kernel_pdist(env, op, p, tol):
     assert rel(ours, orc.evaluate(pts, off, op=oop, p=p, truth=True)) <= tol
 
 
+@pytest.mark.parametrize("kernel", [False, True])
+def test_reference_kernel_sampled_rows_equal_the_full_scatter(env, kernel):
+    """The row-sampled copy-back (used beside the headline bench, where the
+    full triangle is 20 GB) returns the same bits as the full host scatter."""
+    orc, pts, off, dp, do = env
+    n = len(off) - 1
+    full = np.full(n * (n + 1) // 2 if kernel else n * (n - 1) // 2, np.nan, np.float32)
+    orc.ref_gpu_triangle(dp.data_ptr(), do.data_ptr(), n, kernel=kernel, host_out=full,
+                         max_output_elements=300_000)
+    rows = np.array([0, 1, 2, 700, 701, 1499, 350, 1024], np.uint64)
+    ms, tiles, vals, starts = orc.ref_gpu_triangle_rows(dp.data_ptr(), do.data_ptr(), n, rows, kernel=kernel,
+                                                        max_output_elements=300_000)
+    assert tiles > 1 and ms > 0
+    per = 1 if kernel else 0
+    for k, i in enumerate(int(r) for r in rows):
+        lo = i * (i + 1) // 2 if kernel else i * (i - 1) // 2
+        np.testing.assert_array_equal(vals[starts[k]:starts[k + 1]], full[lo:lo + i + per])
+
+
 def test_reference_kernel_l2_kernel(env):
     import stablebear_gb300 as sb
     orc, pts, off, dp, do = env

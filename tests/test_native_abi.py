@@ -34,6 +34,35 @@ def test_every_declared_symbol_is_exported(lib):
         assert name in _native.SIGNATURES, f"{name} has no ctypes signature"
 
 
+def test_alloc_limit_and_counters_need_no_device(lib):
+    from stablebear_gb300 import _native
+    held = lib.sbg_device_bytes_held()
+    count = lib.sbg_device_allocations()
+    assert lib.sbg_set_alloc_limit(0) == 0
+    assert lib.sbg_set_alloc_limit(_native.ALLOC_UNLIMITED) == 0
+    assert lib.sbg_device_bytes_held() == held and lib.sbg_device_allocations() == count
+
+
+def test_every_device_allocation_goes_through_the_counted_allocator():
+    """Only the library's allocator (engine.cu: device_malloc / device_free and
+    their stream-ordered pair) calls the CUDA allocation routines, so the
+    allocation limit and counter see every device allocation.  Checked on the
+    sources, comments stripped."""
+    csrc = os.path.join(ROOT, "stablebear_gb300", "csrc")
+    raw = re.compile(r"\bcuda(Malloc|MallocAsync|MallocManaged|MallocPitch|Malloc3D|MallocArray|Free|FreeAsync)\s*\(")
+    found = {}
+    for f in sorted(os.listdir(csrc)):
+        if not f.endswith((".cu", ".cuh", ".hpp", ".h")):
+            continue
+        text = open(os.path.join(csrc, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        n = len(raw.findall(text))
+        if n:
+            found[f] = n
+    assert found == {"engine.cu": 4}, found
+
+
 def test_version_and_build_type(lib):
     assert lib.sbg_api_version() == 1
     assert lib.sbg_build_type() == b"CUDA"

@@ -137,6 +137,34 @@ def test_rows_subset_matches_full():
         np.testing.assert_array_equal(vals[starts[k]:starts[k + 1]], full[i * (i - 1) // 2: i * (i - 1) // 2 + i])
 
 
+@pytest.mark.parametrize("mode", [orc.MODE_PDIST, orc.MODE_KERNEL])
+def test_chunked_rows_match_whole_rows(mode):
+    """Threads taking pieces of rows (the CPU-baseline schedule) compute the
+    same bits as threads taking whole rows, including rows with no pairs."""
+    from stablebear_gb300 import synthetic
+    pts, off = synthetic.plain_l1(150, seed=5)
+    rows = np.array([0, 1, 2, 149, 63, 64, 65, 100, 0], dtype=np.uint64)
+    op = orc.OP_L2 if mode == orc.MODE_KERNEL else orc.OP_L1
+    whole, s0 = orc.evaluate_rows(pts, off, rows, op=op, mode=mode, threads=3)
+    for chunk in (1, 7, 64, 1000):
+        part, s1 = orc.evaluate_rows(pts, off, rows, op=op, mode=mode, threads=5, chunk=chunk)
+        np.testing.assert_array_equal(s0, s1)
+        np.testing.assert_array_equal(part, whole)
+
+
+def test_timed_builds_match_the_checker():
+    """The -O3 host-CPU build without contraction is bit for bit the checker;
+    with FMA contraction it stays within the f32 parity bound."""
+    from stablebear_gb300 import synthetic
+    pts, off = synthetic.plain_l1(200, seed=6)
+    rows = np.arange(1, 200, 9, dtype=np.uint64)
+    want, _ = orc.evaluate_rows(pts, off, rows)
+    off_, _ = orc.evaluate_rows(pts, off, rows, build="o3_off", chunk=16)
+    fast, _ = orc.evaluate_rows(pts, off, rows, build="o3_fast", chunk=16)
+    np.testing.assert_array_equal(off_, want)
+    assert np.max(np.abs(fast - want) / np.maximum(np.abs(want), 1e-30)) < 1e-5
+
+
 def test_segment_formula_matches_count():
     from stablebear_gb300 import synthetic
     pts, off = synthetic.plain_l1(200, seed=4)

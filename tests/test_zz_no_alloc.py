@@ -7,8 +7,11 @@ only lends buffers).  The test calls it through the C ABI twice in a row and
 checks each result against sbg_pairwise_device, the allocating entry point,
 with the tolerance the other parity tests use (float32: 1e-5 relative; here
 the two paths run the same kernel, so the results are in fact identical).
-It also checks the clear rejection of a problem too large for the fixed
-scratch (the hybrid kernel's packed copy of long PCFs).  This file is collected last so a failure here cannot hide others.
+Both calls run with the library's device-allocation limit at zero, and the
+test checks that the library's allocation counter and the device's free
+memory do not move.  It also checks the clear rejection of a problem too
+large for the fixed scratch (the hybrid kernel's packed copy of long PCFs).
+This file is collected last so a failure here cannot hide others.
 """
 import ctypes
 
@@ -45,14 +48,30 @@ def _run_pair(torch, nat, pts, off, skip, op, p):
     ref = torch.full((count,), float("nan"), dtype=tdt, device="cuda")
     nat.check(nat.lib().sbg_pairwise_device(code, op, p, skip, dp.data_ptr(), do.data_ptr(), n, None, None, 0,
                                             None, None, lmax, ref.data_ptr(), 0, 0, 0, st))
-    outs = []
-    for _ in range(2):  # two calls in a row share the scratch
-        got = torch.full((count,), float("nan"), dtype=tdt, device="cuda")
-        nat.check(nat.lib().sbg_pairwise_device_noalloc(code, op, p, skip, dp.data_ptr(), do.data_ptr(), n,
-                                                        int(off[-1]), None, None, 0, 0, None, None, lmax,
-                                                        got.data_ptr(), 0, 0, 0, st))
-        outs.append(got)
+    outs = [torch.full((count,), float("nan"), dtype=tdt, device="cuda") for _ in range(2)]
     torch.cuda.synchronize()
+    # Both calls run with the library's allocation limit at 0, so any device
+    # allocation through the library's allocator would fail the call; its
+    # allocation counter must not move, and the device's free memory must be
+    # the same before and after the second call (the first may still load
+    # kernels, which the driver does lazily).
+    lib = nat.lib()
+    allocs = lib.sbg_device_allocations()
+    lib.sbg_set_alloc_limit(0)
+    try:
+        for k, got in enumerate(outs):  # two calls in a row share the scratch
+            if k == 1:
+                torch.cuda.synchronize()
+                free_before = torch.cuda.mem_get_info()[0]
+            nat.check(lib.sbg_pairwise_device_noalloc(code, op, p, skip, dp.data_ptr(), do.data_ptr(), n,
+                                                      int(off[-1]), None, None, 0, 0, None, None, lmax,
+                                                      got.data_ptr(), 0, 0, 0, st))
+        torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
+    finally:
+        lib.sbg_set_alloc_limit(nat.ALLOC_UNLIMITED)
+    assert lib.sbg_device_allocations() == allocs
+    assert free_after == free_before
     ref = ref.cpu().numpy().astype(np.float64)
     for got in outs:
         g = got.cpu().numpy().astype(np.float64)
