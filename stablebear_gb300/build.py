@@ -78,7 +78,63 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
         os.replace(LIB + ".tmp", LIB)
     if verbose:
         print(LIB)
+    build_pymodule(force=force, verbose=verbose)
     return LIB
+
+
+# ---- the compiled Python binding (pybind11) ----------------------------------
+
+PYMODULE_SRC = os.path.join(HERE, "pymodule", "sb_module.cpp")
+
+
+def pymodule_path() -> str:
+    import sysconfig
+    return os.path.join(OUT_DIR, "_sb_gb300" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
+
+
+def pybind11_include() -> str | None:
+    """pybind11's headers: the pybind11 package where installed, else the
+    copy PyTorch ships in its include directory (found without importing
+    torch)."""
+    try:
+        import pybind11
+        return pybind11.get_include()
+    except ImportError:
+        pass
+    import importlib.util
+    spec = importlib.util.find_spec("torch")
+    for loc in (spec.submodule_search_locations or []) if spec else []:
+        inc = os.path.join(loc, "include")
+        if os.path.isfile(os.path.join(inc, "pybind11", "pybind11.h")):
+            return inc
+    return None
+
+
+def build_pymodule(force: bool = False, verbose: bool = False) -> str | None:
+    """Compiles ``_sb_gb300`` (host C++ over the C ABI, linked to
+    libsbgpu.so).  Returns its path, or None where pybind11's headers or
+    Python.h are missing (the ctypes binding then serves the same API)."""
+    import sysconfig
+    pyinc = sysconfig.get_paths()["include"]
+    inc = pybind11_include()
+    if inc is None or not os.path.isfile(os.path.join(pyinc, "Python.h")):
+        if verbose:
+            print(f"_sb_gb300 not built: {'no pybind11 headers' if inc is None else 'no Python.h in ' + pyinc}")
+        return None
+    out = pymodule_path()
+    if force or _stale(out, [PYMODULE_SRC, LIB, os.path.join(INCLUDE, "sbgpu.h"), __file__]):
+        cxx = shutil.which("g++") or shutil.which("c++")
+        if cxx is None:
+            raise RuntimeError("no C++ compiler for the _sb_gb300 binding")
+        cmd = [cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-fvisibility=hidden", "-I", pyinc, "-I", inc,
+               "-I", INCLUDE, PYMODULE_SRC, "-L", OUT_DIR, "-lsbgpu", "-Wl,-rpath,$ORIGIN", "-o", out + ".tmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"_sb_gb300 build failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(out + ".tmp", out)
+    if verbose:
+        print(out)
+    return out
 
 
 if __name__ == "__main__":

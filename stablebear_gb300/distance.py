@@ -6,6 +6,8 @@ and ``stablebear/inner_product.py``; the per-dtype backend classes
 ``InnerProduct_f64_f64`` mirror the pybind classes of
 ``src/python/functional/py_distance.cpp:225-250`` and
 ``py_inner_product.cpp:71-90``: static methods returning ``(task, result)``.
+Those classes are the compiled pybind11 module ``_sb_gb300`` where it was
+built (``_binding.py``), else the ctypes classes below, over the same C ABI.
 
 Every computation runs on the GPU through the native library; there is no
 CPU path (``force_cpu`` is accepted and ignored, see ``system.py``).
@@ -16,6 +18,7 @@ import ctypes
 
 import numpy as np
 
+from . import _binding
 from . import _native as nat
 from .matrices import DistanceMatrix, SymmetricMatrix
 from .pcf import Pcf, PcfArray, _has_matching_types, _resolve_pcf_inputs, pcf32, pcf64
@@ -139,6 +142,18 @@ class InnerProduct_f64_f64(_InnerProductBackend):
     _np = np.float64
     _code = nat.F64
 
+
+# The same four classes over ctypes (defined above) and, where it was built,
+# compiled over pybind11 (_sb_gb300): the public names are the compiled ones
+# when present, the ctypes ones otherwise.
+CTYPES_BACKENDS = {"Distance_f32_f32": Distance_f32_f32, "Distance_f64_f64": Distance_f64_f64,
+                   "InnerProduct_f32_f32": InnerProduct_f32_f32, "InnerProduct_f64_f64": InnerProduct_f64_f64}
+_compiled = _binding.compiled()
+if _compiled is not None:
+    Distance_f32_f32 = _compiled.Distance_f32_f32
+    Distance_f64_f64 = _compiled.Distance_f64_f64
+    InnerProduct_f32_f32 = _compiled.InnerProduct_f32_f32
+    InnerProduct_f64_f64 = _compiled.InnerProduct_f64_f64
 
 _DISTANCE_BACKEND_MAP = {pcf32: Distance_f32_f32, pcf64: Distance_f64_f64}
 _INNER_PRODUCT_BACKEND_MAP = {pcf32: InnerProduct_f32_f32, pcf64: InnerProduct_f64_f64}
