@@ -217,6 +217,8 @@ def run_aux(args):
         O = torch.tensor(off.astype(np.int64), device="cuda")
         G = torch.randn(n, n, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
         G = G + G.T
+        segs_kernel = synthetic.segment_count(off, pts, 2)
+        segs_dist = synthetic.segment_count(off, pts, 1)
         for name in ("l2_kernel", "l2"):
             diag = name == "l2_kernel"
 
@@ -233,11 +235,17 @@ def run_aux(args):
                 ms_f = _time_device(fwd, max(5, args.steps), 3)
             ms_fb = _time_device(fwdbwd, max(5, args.steps), 3)
             pairs = n * (n + 1) // 2 if diag else n * (n - 1) // 2
+            # rectangles walked: the forward's; the backward recomputes the same
+            # merge of every off-diagonal pair (the diagonal in closed form)
+            segs = segs_kernel if diag else segs_dist
+            ms_b = ms_fb - ms_f
             rep[name] = {"forward_ms": ms_f, "forward_pairs_per_s": pairs / (ms_f / 1e3),
                          "fwd_bwd_ms": ms_fb, "fwd_bwd_pairs_per_s": pairs / (ms_fb / 1e3),
-                         "backward_over_forward": (ms_fb - ms_f) / ms_f}
+                         "backward_ms": ms_b, "backward_over_forward": ms_b / ms_f,
+                         "forward_rect_per_s": segs / (ms_f / 1e3), "backward_rect_per_s": segs_dist / (ms_b / 1e3),
+                         "backward_rate_vs_forward": (segs_dist / (ms_b / 1e3)) / (segs / (ms_f / 1e3))}
         rep.update({"workload": "N=4096 f32, L~U{16..512}, upstream G symmetric N(0,1); grads w.r.t. values and times",
-                    "segments_kernel": synthetic.segment_count(off, pts, 2)})
+                    "segments_kernel": segs_kernel, "segments_pdist": segs_dist})
     elif args.config == "dense":
         from stablebear_gb300 import device as dev
         n = args.n

@@ -297,6 +297,32 @@ int sbg_pairwise_device_noalloc(int dtype, int op, double p, int skip_mode,
                                 void* out, uint64_t out_base, uint64_t row_begin, uint64_t row_end,
                                 void* stream);
 
+/* ---- launch-shape autotuning for single problems ---------------------------------
+ * No counterpart in the reference, whose block dimension and minimum block
+ * side are user settings (include/sbear/settings.hpp:8-23).
+ *
+ * sbg_autotune_device runs the problem (same arguments as
+ * sbg_pairwise_device over the whole problem, results into out) for a few
+ * (warps per CTA, rows per work item) shapes, times each with CUDA events on
+ * the stream (it synchronises), and caches the fastest under the problem's
+ * key: element type, operation, skip mode and its shape bucket (floor(log2)
+ * of n_rows and of max_points).  Later sbg_pairwise_device /
+ * sbg_pairwise_host / task calls whose key matches use the cached shape
+ * unless sbg_set_tuning fixed warps or rows per item.  These two knobs never
+ * change a result bit (the time-windowed kernel keeps its window cap), so a
+ * cached shape only changes the time.  The search sets the process-wide
+ * tuning while it runs: do not run other calls concurrently with it.
+ * *warps / *rows_per_item receive the shape kept, *best_ms its time per call. */
+int sbg_autotune_device(int dtype, int op, double p, int skip_mode,
+                        const void* row_points, const uint64_t* row_offsets, uint64_t n_rows,
+                        const void* col_points, const uint64_t* col_offsets, uint64_t n_cols,
+                        uint32_t max_points, void* out, void* stream,
+                        int* warps, int* rows_per_item, double* best_ms);
+/* Whether the cache holds a shape for this key (*hit 1 or 0), and which. */
+int sbg_tuning_cache_lookup(int dtype, int op, double p, int skip_mode, uint64_t n_rows, uint32_t max_points,
+                            int* warps, int* rows_per_item, int* hit);
+int sbg_tuning_cache_clear(void);
+
 /* The processing order sbg_pairwise_device uses when it picks one itself:
  * perm[i] is the index of the PCF visited i-th, by breakpoint count within
  * each window of 1024 consecutive PCFs (ties by index).  Device pointers,

@@ -83,6 +83,11 @@ SIGNATURES = {
     "sbg_batch_destroy": (None, [_P]),
     "sbg_output_count": (_U64, [_I, _U64, _U64]),
     "sbg_kernel_launches": (_U64, []),
+    "sbg_autotune_device": (_I, [_I, _I, _D, _I, _P, _P, _U64, _P, _P, _U64, ctypes.c_uint32, _P, _P,
+                                 ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D)]),
+    "sbg_tuning_cache_lookup": (_I, [_I, _I, _D, _I, _U64, ctypes.c_uint32, ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                     ctypes.POINTER(_I)]),
+    "sbg_tuning_cache_clear": (_I, []),
     "sbg_set_alloc_limit": (_I, [_U64]),
     "sbg_device_allocations": (_U64, []),
     "sbg_device_bytes_held": (_U64, []),

@@ -274,6 +274,150 @@ namespace sbg
     }
   }
 
+  // The default backward: the same walk, work items, gradient buffers and
+  // arithmetic as SIDE 0 above, with a lean step.  Both sides hold their
+  // current element and the next one in registers (a one-element
+  // lookahead), so the time-gradient term of a breakpoint, which needs the
+  // values on both sides of it, is formed from registers while the load of
+  // the element after next is in flight; the indices are 32-bit offsets
+  // into the packed layout (one address computation per load); every load
+  // and add is predicated, and the loop is unrolled.  SIDE 0 issued about
+  // 98 instructions per warp-step (ncu, N = 4096 L2 kernel).
+  template <typename T, int OP>
+  __global__ void __launch_bounds__(1024) pairs_backward_lean_kernel(const __grid_constant__ BwdParams<T> B)
+  {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sgrad_all = reinterpret_cast<T*>(smem_raw);
+    __shared__ unsigned long long s_item;
+    __shared__ unsigned int s_next_row;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    T* sgv = sgrad_all + (size_t)warp * B.row_cap * 2;
+    T* sgt = sgv + B.row_cap;
+    const unsigned FULL = 0xffffffffu;
+
+    for (;;)
+    {
+      if (threadIdx.x == 0)
+      {
+        s_item = atomicAdd(B.queue, 1ull);
+        s_next_row = 0;
+      }
+      __syncthreads();
+      const unsigned long long item = s_item;
+      if (item >= B.total_items) break;
+      const uint64_t G = ceil_div_u64(B.n, 32);
+      uint64_t c, g;
+      tri_decode(item, 0, B.n, B.q, G, &c, &g);
+      uint64_t row_lo = c * 32ull * B.q;
+      uint64_t row_hi = row_lo + 32ull * B.q;
+      if (row_hi > B.n) row_hi = B.n;
+      const uint64_t col0 = 32ull * g;
+      if (row_lo < col0 + 1) row_lo = col0 + 1;  // the diagonal is handled by diag_backward_kernel
+
+      const uint64_t cj = col0 + lane;
+      const bool cvalid = cj < B.n;
+      uint64_t corig = B.perm ? B.perm[cvalid ? cj : col0] : (cvalid ? cj : col0);
+      if (corig >= B.n) corig = 0;  // never expected: the order is a permutation
+      const uint64_t coff = B.off[corig];
+      const uint32_t clen = (uint32_t)(B.off[corig + 1] - coff);
+      const uint32_t maxlc = __reduce_max_sync(FULL, clen);
+      const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > B.npts);
+      if (item_ok)
+      {
+        const Elem<T>* col = B.pk + coff;
+        T* cgrad = B.grad + 2 * coff;
+        for (;;)
+        {
+          unsigned r = 0;
+          if (lane == 0) r = atomicAdd(&s_next_row, 1u);
+          r = __shfl_sync(FULL, r, 0);
+          const uint64_t i = row_lo + r;
+          if (i >= row_hi) break;
+          const uint64_t iorig = B.perm ? B.perm[i] : i;
+          if (iorig >= B.n) continue;  // never expected: the order is a permutation
+          const uint64_t roff = B.off[iorig];
+          const uint32_t rlen = (uint32_t)(B.off[iorig + 1] - roff);
+          if (rlen == 0 || rlen > B.row_cap || roff + rlen > B.npts) continue;
+          T w = T(0);
+          if (cvalid && cj < i)
+          {
+            const uint64_t idx = condensed_index(B.mode, iorig, corig);
+            w = B.grad_out[idx];
+            if (OP == BWD_L2DIST)
+            {
+              const T D = B.fwd[idx];
+              w = D > T(0) ? w / D : T(0);
+            }
+          }
+          if (!__any_sync(FULL, w != T(0))) continue;
+          for (uint32_t k = lane; k < rlen; k += 32) { sgv[k] = T(0); sgt[k] = T(0); }
+          __syncwarp();
+
+          const Elem<T>* row = B.pk + roff;
+          const bool live = w != T(0);
+          Elem<T> F = row[0], F2 = row[rlen > 1 ? 1 : 0];
+          Elem<T> Gc = col[0], G2 = col[clen > 1 ? 1 : 0];
+          uint32_t fi = 0, gi = 0;
+          T t = T(0), accF = T(0), accG = T(0);
+          const uint32_t steps = rlen + maxlc - 1;
+#pragma unroll 4
+          for (uint32_t s = 0; s < steps; ++s)
+          {
+            const bool takeF = row_first(F.tn, Gc.tn);
+            const T tn = takeF ? F.tn : Gc.tn;
+            const T dt = tn - t;
+            T cf, cg;
+            seg_coeffs<OP>(F.v, Gc.v, cf, cg);
+            accF = fma(dt, cf, accF);
+            accG = fma(dt, cg, accG);
+            // The row stays on its last element once exhausted (it then runs
+            // to TMAX); Gc.tn < F.tn <= TMAX when the column moves, so the
+            // column has a next element and G2 is it.
+            const bool advF = takeF && fi + 1 < rlen;
+            const bool advG = !takeF;
+            const T dF = (F.tn == Gc.tn) ? T(0) : w * step_delta<OP>(F.v, F2.v, Gc.v);
+            const T dG = (dt == T(0)) ? T(0) : w * step_delta<OP>(Gc.v, G2.v, F.v);
+            if (advF && live)
+            {
+              atomicAdd(&sgv[fi], w * accF);
+              atomicAdd(&sgt[fi], dF);
+            }
+            if (advG && live) red_add2(&cgrad[2 * (size_t)gi], w * accG, dG);
+            if (advF)
+            {
+              F = F2;
+              ++fi;
+              F2 = row[min(fi + 1, rlen - 1)];
+              accF = T(0);
+            }
+            if (advG)
+            {
+              Gc = G2;
+              ++gi;
+              G2 = col[min(gi + 1, clen - 1)];
+              accG = T(0);
+            }
+            t = tn;
+          }
+          if (live)
+          {
+            atomicAdd(&sgv[fi], w * accF);
+            atomicAdd(&cgrad[2 * (size_t)gi], w * accG);
+          }
+          __syncwarp();
+          for (uint32_t k = lane; k < rlen; k += 32)
+          {
+            const T gv = sgv[k], gt = sgt[k];
+            if (gv != T(0) || gt != T(0)) red_add2(&B.grad[2 * (roff + k)], gv, gt);
+          }
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+    }
+  }
+
   // (dL/dv_k, dL/dt_{k+1}) slots to the point layout (dL/dt_k, dL/dv_k).
   // The slot of a PCF's last element holds no time gradient (there is no
   // breakpoint after it).  One warp per PCF.
@@ -323,6 +467,15 @@ namespace sbg
         }
       }
     }
+  }
+
+  constexpr bool defined_stage_columns()
+  {
+#if defined(SBG_BWD_STAGE_COLUMNS)
+    return true;
+#else
+    return false;
+#endif
   }
 
   template <typename T>
@@ -417,9 +570,19 @@ namespace sbg
     SBG_CUDA(cudaMemsetAsync(queue, 0, 8, st));
     if (B.total_items > 0)
     {
-      void (*fn)(const BwdParams<T>) = bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SIDE, WI>
-                                     : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SIDE, WI>
-                                                         : pairs_backward_kernel<T, BWD_L1DIST, SIDE, WI>;
+#if !defined(SBG_BWD_LEGACY)
+      // the lean step (same walk and arithmetic) unless an alternative is asked for
+      constexpr bool LEAN = SIDE == 0 && !WI && !defined_stage_columns();
+#else
+      constexpr bool LEAN = false;
+#endif
+      void (*fn)(const BwdParams<T>) =
+          LEAN ? (bop == BWD_INNER ? pairs_backward_lean_kernel<T, BWD_INNER>
+                  : bop == BWD_L2DIST ? pairs_backward_lean_kernel<T, BWD_L2DIST>
+                                      : pairs_backward_lean_kernel<T, BWD_L1DIST>)
+               : (bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SIDE, WI>
+                  : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SIDE, WI>
+                                      : pairs_backward_kernel<T, BWD_L1DIST, SIDE, WI>);
       SBG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms);
       fn<<<grid, warps * 32, smem, st>>>(B);

@@ -463,3 +463,135 @@ extern "C"
     });
   }
 }
+
+namespace
+{
+  // Restores the process-wide (warps, rows per item) settings on scope exit.
+  struct ShapeOverride
+  {
+    int warps = sbg::settings().warps.load(), chunk = sbg::settings().rowChunk.load();
+    ~ShapeOverride()
+    {
+      sbg::settings().warps.store(warps);
+      sbg::settings().rowChunk.store(chunk);
+    }
+  };
+
+  template <typename T>
+  void autotune_device(int skip_mode, int op, double p, const sbg::PcfSet<T>& r, const sbg::PcfSet<T>* c,
+                       uint32_t max_points, T* out, cudaStream_t st, int* best_w, int* best_q, double* best_ms)
+  {
+    using namespace sbg;
+    const int opk = op_kind(op, p);
+    const DeviceInfo dev = device_info();
+    const uint64_t nc = skip_mode == SBG_SKIP_NONE ? c->n : r.n;
+    LengthStats ls;
+    ls.lmax = max_points; ls.lmin = 1; ls.mean = max_points;
+    const Plan base = make_plan<T>(skip_mode, r.n, nc, ls, ls, dev, -1);
+    std::vector<std::pair<int, int>> cands;
+    for (int w : {16, 24, 32})
+      for (uint32_t q : {base.q / 4, base.q / 2, base.q, base.q * 2})
+        if (q >= 1 && q <= 32) cands.push_back({w, (int)q});
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SBG_CUDA(cudaEventCreate(&e0));
+    SBG_CUDA(cudaEventCreate(&e1));
+    struct Events
+    {
+      cudaEvent_t a, b;
+      ~Events() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } ev{e0, e1};
+    ShapeOverride restore;
+    double best = 1e300;
+    int bw = base.warps, bq = (int)base.q;
+    for (const auto& cand : cands)
+    {
+      settings().warps.store(cand.first);
+      settings().rowChunk.store(cand.second);
+      try
+      {
+        compute_device<T>(skip_mode, op, p, r, c, nullptr, nullptr, max_points, out, 0, 0, r.n, st);  // warm-up
+        SBG_CUDA(cudaEventRecord(e0, st));
+        for (int k = 0; k < 2; ++k)
+          compute_device<T>(skip_mode, op, p, r, c, nullptr, nullptr, max_points, out, 0, 0, r.n, st);
+        SBG_CUDA(cudaEventRecord(e1, st));
+        SBG_CUDA(cudaEventSynchronize(e1));
+      }
+      catch (const Error& e)
+      {
+        if (e.status != ST_INVALID_ARGUMENT) throw;  // a shape that does not fit: skip it
+        continue;
+      }
+      float ms = 0.f;
+      SBG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms / 2 < best)
+      {
+        best = ms / 2;
+        bw = cand.first;
+        bq = cand.second;
+      }
+    }
+    tune_cache_put(tune_key((int)sizeof(T), opk, skip_mode, r.n, max_points), bw, bq);
+    if (best_w) *best_w = bw;
+    if (best_q) *best_q = bq;
+    if (best_ms) *best_ms = best;
+  }
+}
+
+extern "C"
+{
+  int sbg_autotune_device(int dtype, int op, double p, int skip_mode, const void* row_points,
+                          const uint64_t* row_offsets, uint64_t n_rows, const void* col_points,
+                          const uint64_t* col_offsets, uint64_t n_cols, uint32_t max_points, void* out, void* stream,
+                          int* warps, int* rows_per_item, double* best_ms)
+  {
+    using namespace sbg;
+    return guarded([&] {
+      check_common(dtype, op, p, skip_mode);
+      check_set(row_points, row_offsets, n_rows);
+      if (skip_mode == SBG_SKIP_NONE) check_set(col_points, col_offsets, n_cols);
+      if (max_points == 0) throw Error(ST_INVALID_ARGUMENT, "max_points must be given");
+      if (output_count(skip_mode, n_rows, n_cols) == 0) throw Error(ST_INVALID_ARGUMENT, "empty problem");
+      if (!out) throw Error(ST_INVALID_ARGUMENT, "null output");
+      (void)current_device();
+      cudaStream_t st = static_cast<cudaStream_t>(stream);
+      int w = 0, q = 0;
+      if (dtype == SBG_F32)
+      {
+        PcfSet<float> r{static_cast<const float*>(row_points), row_offsets, n_rows};
+        PcfSet<float> c{static_cast<const float*>(col_points), col_offsets, n_cols};
+        autotune_device<float>(skip_mode, op, p, r, skip_mode == SBG_SKIP_NONE ? &c : nullptr, max_points,
+                               static_cast<float*>(out), st, &w, &q, best_ms);
+      }
+      else
+      {
+        PcfSet<double> r{static_cast<const double*>(row_points), row_offsets, n_rows};
+        PcfSet<double> c{static_cast<const double*>(col_points), col_offsets, n_cols};
+        autotune_device<double>(skip_mode, op, p, r, skip_mode == SBG_SKIP_NONE ? &c : nullptr, max_points,
+                                static_cast<double*>(out), st, &w, &q, best_ms);
+      }
+      if (warps) *warps = w;
+      if (rows_per_item) *rows_per_item = 32 * q;
+    });
+  }
+
+  int sbg_tuning_cache_lookup(int dtype, int op, double p, int skip_mode, uint64_t n_rows, uint32_t max_points,
+                              int* warps, int* rows_per_item, int* hit)
+  {
+    using namespace sbg;
+    return guarded([&] {
+      check_common(dtype, op, p, skip_mode);
+      if (!hit) throw Error(ST_INVALID_ARGUMENT, "null hit pointer");
+      int w = 0, q = 0;
+      *hit = tune_cache_get(tune_key(dtype == SBG_F32 ? 4 : 8, op_kind(op, p), skip_mode, n_rows, max_points), &w, &q)
+                 ? 1 : 0;
+      if (warps) *warps = *hit ? w : 0;
+      if (rows_per_item) *rows_per_item = *hit ? 32 * q : 0;
+    });
+  }
+
+  int sbg_tuning_cache_clear(void)
+  {
+    sbg::tune_cache_clear();
+    return SBG_OK;
+  }
+}

@@ -278,8 +278,48 @@ namespace sbg
     return problem_item_count(d);
   }
 
+  // ---- launch-shape cache (sbg_autotune_device) ---------------------------------
+
+  static std::mutex g_tune_mu;
+  static std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+
+  static int floor_log2(uint64_t x)
+  {
+    int r = -1;
+    while (x) { x >>= 1; ++r; }
+    return r;
+  }
+
+  TuneKey tune_key(int elem_bytes, int opk, int mode, uint64_t n, uint32_t lmax)
+  {
+    return TuneKey{elem_bytes, opk, mode, floor_log2(n), floor_log2(lmax)};
+  }
+
+  bool tune_cache_get(const TuneKey& k, int* warps, int* q)
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(k);
+    if (it == g_tune_cache.end()) return false;
+    *warps = it->second.first;
+    *q = it->second.second;
+    return true;
+  }
+
+  void tune_cache_put(const TuneKey& k, int warps, int q)
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[k] = {warps, q};
+  }
+
+  void tune_cache_clear()
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache.clear();
+  }
+
   template <typename T>
-  Plan make_plan(int mode, uint64_t nr, uint64_t nc, const LengthStats& rs, const LengthStats& cs, const DeviceInfo& dev)
+  Plan make_plan(int mode, uint64_t nr, uint64_t nc, const LengthStats& rs, const LengthStats& cs, const DeviceInfo& dev,
+                 int opk)
   {
     Plan pl;
     const int U = kernel_unroll(sizeof(T) == 8);
@@ -404,6 +444,36 @@ namespace sbg
         fit = window_layout(pl, es, w, 32 * q, std::max(lmax_r, lmax_c), usable);
       if (!fit) throw Error(ST_INVALID_ARGUMENT, "time-windowed variant: the window setting does not fit in shared memory");
     }
+    // A launch shape sbg_autotune_device measured for problems of this
+    // shape bucket, unless the caller fixed warps or rows per item.  Only
+    // the warps and rows per item change; the time-windowed kernel keeps the
+    // window cap of the default plan, so no result changes by a bit.
+    if (opk >= 0 && settings().warps.load() == 0 && settings().rowChunk.load() == 0)
+    {
+      int tw = 0, tq = 0;
+      if (tune_cache_get(tune_key((int)sizeof(T), opk, mode, nr, std::max(lmax_r, lmax_c)), &tw, &tq) && tw > 0 &&
+          tq > 0 && tq <= 32)
+      {
+        Plan trial = pl;
+        bool ok = true;
+        if (pl.kvar == 6)
+          ok = window_layout(trial, es, tw, 32u * (uint32_t)tq, std::max(lmax_r, lmax_c), usable, pl.win_r);
+        else if (pl.kvar == 5 || pl.kvar == 1 || pl.kvar == 2)
+        {
+          ok = smem_for(tw) <= usable;
+          trial.warps = tw;
+          trial.smem_bytes = smem_for(tw);
+        }
+        else
+          trial.warps = tw;
+        if (ok)
+        {
+          trial.q = (uint32_t)tq;
+          pl = trial;
+          q = pl.q;
+        }
+      }
+    }
     const uint64_t items = items_for(mode, 0, nr, nc, q);
     const int per_sm = (pl.kvar == 0) ? 2 : ctas_per_sm(dev, pl.warps, pl.smem_bytes);
     pl.grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(items, (uint64_t)dev.sms * per_sm));
@@ -435,8 +505,10 @@ namespace sbg
     return true;
   }
 
-  template Plan make_plan<float>(int, uint64_t, uint64_t, const LengthStats&, const LengthStats&, const DeviceInfo&);
-  template Plan make_plan<double>(int, uint64_t, uint64_t, const LengthStats&, const LengthStats&, const DeviceInfo&);
+  template Plan make_plan<float>(int, uint64_t, uint64_t, const LengthStats&, const LengthStats&, const DeviceInfo&,
+                                  int);
+  template Plan make_plan<double>(int, uint64_t, uint64_t, const LengthStats&, const LengthStats&, const DeviceInfo&,
+                                   int);
 
   static LengthStats host_length_stats(const uint64_t* off, uint64_t n)
   {
@@ -576,7 +648,7 @@ namespace sbg
     ls.lmax = lmax;
     ls.lmin = 1;
     ls.mean = lmax;
-    const Plan pl = make_plan<T>(mode, rows.n, cs.n, ls, ls, dev);
+    const Plan pl = make_plan<T>(mode, rows.n, cs.n, ls, ls, dev, opk);
     if (row_begin % (32ull * pl.q) != 0)
       throw Error(ST_INVALID_ARGUMENT, "row_begin must be a multiple of the row chunk (32*q)");
 
@@ -663,7 +735,7 @@ namespace sbg
     const DeviceInfo dev = device_info();
     LengthStats ls;
     ls.lmax = lmax; ls.lmin = 1; ls.mean = lmax;
-    const Plan pl = make_plan<T>(mode, n_rows, mode == MODE_CROSS ? n_cols : n_rows, ls, ls, dev);
+    const Plan pl = make_plan<T>(mode, n_rows, mode == MODE_CROSS ? n_cols : n_rows, ls, ls, dev, -1);
     size_t need = 256;  // work-queue counter
     if (pl.packed)
     {
@@ -688,7 +760,7 @@ namespace sbg
     const int opk = op_kind(op, p);
     LengthStats ls;
     ls.lmax = lmax; ls.lmin = 1; ls.mean = lmax;
-    const Plan pl = make_plan<T>(mode, rows.n, cs.n, ls, ls, dev);
+    const Plan pl = make_plan<T>(mode, rows.n, cs.n, ls, ls, dev, opk);
     if (row_begin % (32ull * pl.q) != 0)
       throw Error(ST_INVALID_ARGUMENT, "row_begin must be a multiple of the row chunk (32*q)");
     const size_t need = scratch_needed<T>(mode, rows.n, cs.n, lmax, row_points, col_points);
@@ -825,7 +897,7 @@ namespace sbg
       }
     }
 
-    const Plan pl = make_plan<T>(mode, rows.n, cs.n, rstat, cstat, dev);
+    const Plan pl = make_plan<T>(mode, rows.n, cs.n, rstat, cstat, dev, op_kind(op, p));
     const uint64_t chunk_rows = 32ull * pl.q;
 
     // Output route.  Direct: on coherent hosts (Grace + NVLink-C2C, where the

@@ -11,6 +11,7 @@
 #include <functional>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -156,8 +157,9 @@ namespace sbg
   };
 
   template <typename T>
+  // opk: the operation kind, for the launch-shape cache (-1: no lookup).
   Plan make_plan(int mode, uint64_t n_rows, uint64_t n_cols, const LengthStats& rows, const LengthStats& cols,
-                 const DeviceInfo& dev);
+                 const DeviceInfo& dev, int opk);
 
   int op_kind(int op, double p);
 
@@ -244,6 +246,25 @@ namespace sbg
   void set_alloc_limit(uint64_t bytes);
   uint64_t device_allocations();
   uint64_t device_bytes_held();
+
+  // Launch-shape cache of the single-problem planner, filled by
+  // sbg_autotune_device.  Key: element size, operation, mode and the
+  // problem's shape bucket (floor(log2) of the PCF count and of the longest
+  // PCF).  Value: warps per CTA and rows per work item (32 q), the two knobs
+  // that change no bit of a result.
+  struct TuneKey
+  {
+    int elem_bytes, opk, mode, n_log2, lmax_log2;
+    bool operator<(const TuneKey& o) const
+    {
+      return std::tie(elem_bytes, opk, mode, n_log2, lmax_log2) <
+             std::tie(o.elem_bytes, o.opk, o.mode, o.n_log2, o.lmax_log2);
+    }
+  };
+  TuneKey tune_key(int elem_bytes, int opk, int mode, uint64_t n, uint32_t lmax);
+  bool tune_cache_get(const TuneKey& k, int* warps, int* q);
+  void tune_cache_put(const TuneKey& k, int warps, int q);
+  void tune_cache_clear();
 
   // RAII stream-ordered device buffer (device_malloc_async / device_free_async).
   class StreamBuffer

@@ -43,6 +43,18 @@ def test_alloc_limit_and_counters_need_no_device(lib):
     assert lib.sbg_device_bytes_held() == held and lib.sbg_device_allocations() == count
 
 
+def test_tuning_cache_needs_no_device(lib):
+    hit, w, r = ctypes.c_int(-1), ctypes.c_int(-1), ctypes.c_int(-1)
+    assert lib.sbg_tuning_cache_clear() == 0
+    assert lib.sbg_tuning_cache_lookup(0, 0, 1.0, 1, 1000, 200, ctypes.byref(w), ctypes.byref(r),
+                                       ctypes.byref(hit)) == 0
+    assert hit.value == 0 and w.value == 0 and r.value == 0
+    assert lib.sbg_tuning_cache_lookup(0, 1, 0.5, 1, 1000, 200, None, None, ctypes.byref(hit)) == -1  # p < 1
+    # the autotuner checks its arguments before any CUDA call
+    assert lib.sbg_autotune_device(0, 0, 1.0, 1, None, None, 10, None, None, 0, 0, None, None, None, None,
+                                   None) == -1
+
+
 def test_every_device_allocation_goes_through_the_counted_allocator():
     """Only the library's allocator (engine.cu: device_malloc / device_free and
     their stream-ordered pair) calls the CUDA allocation routines, so the
