@@ -48,8 +48,12 @@ def parse():
                     help="skip the reference's own CUDA kernel on the same problem after the timed region")
     ap.add_argument("--order", type=int, default=0, choices=[0, 1],
                     help="processing order of the device entry: 0 length order (default), 1 caller order")
-    ap.add_argument("--variant", type=int, default=0, choices=range(0, 7),
-                    help="kernel variant of the engine (0 automatic; 4 hybrid, 5 shared memory, 6 time-windowed)")
+    ap.add_argument("--variant", type=int, default=0, choices=range(0, 9),
+                    help="kernel variant of the engine (0 automatic; 4 hybrid, 5 shared memory, 6 time-windowed; "
+                         "7 replicated row with one unified load per step, 8 merge path: measurement only)")
+    ap.add_argument("--lengths", default="",
+                    help="LO:HI: breakpoint counts ~ U{LO..HI} instead of the headline's Poisson(256)+2 "
+                         "(a measurement workload, not the headline)")
     ap.add_argument("--window-cap", type=int, default=0,
                     help="time-windowed kernel: elements of a PCF per window (0 automatic)")
     ap.add_argument("--config", default="large",
@@ -286,10 +290,23 @@ def dist_env():
     return ws, rank, local
 
 
+LENGTHS = ""  # --lengths LO:HI (a measurement workload); empty: the headline's Poisson(256)+2
+
+
 def workload(n, seed):
     from stablebear_gb300 import synthetic
+    if LENGTHS:
+        lo, hi = (int(x) for x in LENGTHS.split(":"))
+        return synthetic.gaussian(n, synthetic.uniform_lengths(lo, hi), np.float32, seed)
     pts, off = synthetic.large_l1(n, seed=seed)
     return pts, off
+
+
+def lengths_text():
+    if LENGTHS:
+        lo, hi = LENGTHS.split(":")
+        return f"L~U{{{lo}..{hi}}}"
+    return "L~Poisson(256)+2"
 
 
 def _generator_hash():
@@ -301,7 +318,7 @@ def _generator_hash():
 
 
 def config(args, n, ws):
-    return {"workload": f"L1 pdist, N={n} float32 PCFs, L~Poisson(256)+2, N(0,1) values, Exp(1) gaps, seed=0",
+    return {"workload": f"L1 pdist, N={n} float32 PCFs, {lengths_text()}, N(0,1) values, Exp(1) gaps, seed=0",
             "n_pcfs": n, "pairs_per_step": n * (n - 1) // 2,
             "output": "condensed DistanceMatrix float32 kept in HBM",
             "l2": "inputs (CSR) and output larger than L2; no flush",
@@ -574,7 +591,9 @@ def run_reference(args, ws, rank):
 # ---- GPU arm -------------------------------------------------------------------
 
 def main():
+    global LENGTHS
     args = parse()
+    LENGTHS = args.lengths
     ws, rank, local = dist_env()
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -96,7 +96,10 @@ int sbg_get_device_verbose(void);
  * rows read through L1, 5 shared-memory with the row as separate time and
  * value arrays, the automatic choice when the PCFs fit, 6 time-windowed
  * shared memory: each work item walks time windows holding at most a cap of
- * elements of every PCF, the automatic choice for longer PCFs), order
+ * elements of every PCF, the automatic choice for longer PCFs; 7 and 8,
+ * float32 only and never automatic, kept to measure two other designs: 7
+ * one unified shared-memory load per step from a row replicated 16 times, 8
+ * merge path with one pair per warp), order
  * (1 caller's, 2 sorted
  * by breakpoint count), output bytes per pipeline band (automatic: 1/8 of
  * the output, the last eighth cut into halving parts so that little of the
@@ -321,6 +324,12 @@ int sbg_autotune_device(int dtype, int op, double p, int skip_mode,
 /* Whether the cache holds a shape for this key (*hit 1 or 0), and which. */
 int sbg_tuning_cache_lookup(int dtype, int op, double p, int skip_mode, uint64_t n_rows, uint32_t max_points,
                             int* warps, int* rows_per_item, int* hit);
+/* Pins a shape for a key by hand (e.g. a table saved from an earlier
+ * process): warps in [1, 32], rows_per_item a multiple of 32 in [32, 1024].
+ * A shape that does not fit the problem's shared memory is ignored when
+ * planning. */
+int sbg_tuning_cache_store(int dtype, int op, double p, int skip_mode, uint64_t n_rows, uint32_t max_points,
+                           int warps, int rows_per_item);
 int sbg_tuning_cache_clear(void);
 
 /* The processing order sbg_pairwise_device uses when it picks one itself:

@@ -87,6 +87,7 @@ SIGNATURES = {
                                  ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_D)]),
     "sbg_tuning_cache_lookup": (_I, [_I, _I, _D, _I, _U64, ctypes.c_uint32, ctypes.POINTER(_I), ctypes.POINTER(_I),
                                      ctypes.POINTER(_I)]),
+    "sbg_tuning_cache_store": (_I, [_I, _I, _D, _I, _U64, ctypes.c_uint32, _I, _I]),
     "sbg_tuning_cache_clear": (_I, []),
     "sbg_set_alloc_limit": (_I, [_U64]),
     "sbg_device_allocations": (_U64, []),

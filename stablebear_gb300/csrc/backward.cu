@@ -274,26 +274,28 @@ namespace sbg
     }
   }
 
-  // The default backward: the same walk, work items, gradient buffers and
-  // arithmetic as SIDE 0 above, with a lean step.  Both sides hold their
-  // current element and the next one in registers (a one-element
-  // lookahead), so the time-gradient term of a breakpoint, which needs the
-  // values on both sides of it, is formed from registers while the load of
-  // the element after next is in flight; the indices are 32-bit offsets
-  // into the packed layout (one address computation per load); every load
-  // and add is predicated, and the loop is unrolled.  SIDE 0 issued about
-  // 98 instructions per warp-step (ncu, N = 4096 L2 kernel).
+  // The default backward: row-synchronous.  The walk above is free-running:
+  // each lane's row advances at its own step, so each lane adds its part of
+  // a row element's gradient into the warp's shared buffer with two float
+  // atomics, and lanes at the same row position contend for the same slot
+  // (the bound: about 46 SM cycles per warp-step at N = 4096).  Here the
+  // warp steps through the row one element at a time, all lanes together:
+  // for row element k each lane first walks its column's breakpoints before
+  // the row's next one (a loop that runs as long as any lane has one), then
+  // all lanes take the row's breakpoint, and the 32 lanes' value-gradient
+  // and time-gradient terms for element k are summed by a shuffle tree and
+  // added to global memory once.  Column gradients leave as in the walk
+  // above, one vector reduction per column breakpoint.  The rectangles, the
+  // per-rectangle terms and the tie rules (ties go to the row; a breakpoint
+  // shared by both PCFs gets no time gradient) are those of the walk; only
+  // the order in which the 32 lanes' terms of a row element are added
+  // changes.  No shared memory.
   template <typename T, int OP>
-  __global__ void __launch_bounds__(1024) pairs_backward_lean_kernel(const __grid_constant__ BwdParams<T> B)
+  __global__ void __launch_bounds__(1024) pairs_backward_rowsync_kernel(const __grid_constant__ BwdParams<T> B)
   {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sgrad_all = reinterpret_cast<T*>(smem_raw);
     __shared__ unsigned long long s_item;
     __shared__ unsigned int s_next_row;
     const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    T* sgv = sgrad_all + (size_t)warp * B.row_cap * 2;
-    T* sgt = sgv + B.row_cap;
     const unsigned FULL = 0xffffffffu;
 
     for (;;)
@@ -321,7 +323,6 @@ namespace sbg
       if (corig >= B.n) corig = 0;  // never expected: the order is a permutation
       const uint64_t coff = B.off[corig];
       const uint32_t clen = (uint32_t)(B.off[corig + 1] - coff);
-      const uint32_t maxlc = __reduce_max_sync(FULL, clen);
       const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > B.npts);
       if (item_ok)
       {
@@ -338,7 +339,7 @@ namespace sbg
           if (iorig >= B.n) continue;  // never expected: the order is a permutation
           const uint64_t roff = B.off[iorig];
           const uint32_t rlen = (uint32_t)(B.off[iorig + 1] - roff);
-          if (rlen == 0 || rlen > B.row_cap || roff + rlen > B.npts) continue;
+          if (rlen == 0 || roff + rlen > B.npts) continue;
           T w = T(0);
           if (cvalid && cj < i)
           {
@@ -350,68 +351,79 @@ namespace sbg
               w = D > T(0) ? w / D : T(0);
             }
           }
-          if (!__any_sync(FULL, w != T(0))) continue;
-          for (uint32_t k = lane; k < rlen; k += 32) { sgv[k] = T(0); sgt[k] = T(0); }
-          __syncwarp();
+          // lanes with no weight take no part in the walk
+          const bool live = w != T(0);
+          if (!__any_sync(FULL, live)) continue;
 
           const Elem<T>* row = B.pk + roff;
-          const bool live = w != T(0);
-          Elem<T> F = row[0], F2 = row[rlen > 1 ? 1 : 0];
-          Elem<T> Gc = col[0], G2 = col[clen > 1 ? 1 : 0];
-          uint32_t fi = 0, gi = 0;
-          T t = T(0), accF = T(0), accG = T(0);
-          const uint32_t steps = rlen + maxlc - 1;
-#pragma unroll 4
-          for (uint32_t s = 0; s < steps; ++s)
+          Elem<T> F = row[0];
+          Elem<T> Gc = col[0];
+          uint32_t gi = 0;
+          T t = T(0), accG = T(0);
+          for (uint32_t k = 0; k < rlen; ++k)
           {
-            const bool takeF = row_first(F.tn, Gc.tn);
-            const T tn = takeF ? F.tn : Gc.tn;
-            const T dt = tn - t;
-            T cf, cg;
-            seg_coeffs<OP>(F.v, Gc.v, cf, cg);
-            accF = fma(dt, cf, accF);
-            accG = fma(dt, cg, accG);
-            // The row stays on its last element once exhausted (it then runs
-            // to TMAX); Gc.tn < F.tn <= TMAX when the column moves, so the
-            // column has a next element and G2 is it.
-            const bool advF = takeF && fi + 1 < rlen;
-            const bool advG = !takeF;
-            const T dF = (F.tn == Gc.tn) ? T(0) : w * step_delta<OP>(F.v, F2.v, Gc.v);
-            const T dG = (dt == T(0)) ? T(0) : w * step_delta<OP>(Gc.v, G2.v, F.v);
-            if (advF && live)
+            const Elem<T> Fn = row[min(k + 1, rlen - 1)];  // the same address in every lane
+            T accF = T(0);
+            // this lane's column breakpoints before the row's next one (ties
+            // go to the row); Gc.tn < F.tn <= TMAX, so the column has a next
+            // element
+            for (;;)
             {
-              atomicAdd(&sgv[fi], w * accF);
-              atomicAdd(&sgt[fi], dF);
+              const bool adv = live && Gc.tn < F.tn;
+              if (!__any_sync(FULL, adv)) break;
+              if (adv)
+              {
+                const T dt = Gc.tn - t;
+                T cf, cg;
+                seg_coeffs<OP>(F.v, Gc.v, cf, cg);
+                accF = fma(dt, cf, accF);
+                accG = fma(dt, cg, accG);
+                const Elem<T> Gn = col[gi + 1];
+                red_add2(&cgrad[2 * (size_t)gi], w * accG,
+                         dt == T(0) ? T(0) : w * step_delta<OP>(Gc.v, Gn.v, F.v));
+                accG = T(0);
+                t = Gc.tn;
+                Gc = Gn;
+                ++gi;
+              }
             }
-            if (advG && live) red_add2(&cgrad[2 * (size_t)gi], w * accG, dG);
-            if (advF)
+            // the row's breakpoint (for its last element, the last rectangle to TMAX)
+            T rowT = T(0);
+            if (live)
             {
-              F = F2;
-              ++fi;
-              F2 = row[min(fi + 1, rlen - 1)];
-              accF = T(0);
+              const T dt = F.tn - t;
+              T cf, cg;
+              seg_coeffs<OP>(F.v, Gc.v, cf, cg);
+              accF = fma(dt, cf, accF);
+              accG = fma(dt, cg, accG);
+              if (k + 1 < rlen)
+              {
+                if (Gc.tn == F.tn)
+                {
+                  // the column's breakpoint coincides: it moves too, and
+                  // neither breakpoint gets a time gradient
+                  const Elem<T> Gn = col[min(gi + 1, clen - 1)];
+                  red_add2(&cgrad[2 * (size_t)gi], w * accG, T(0));
+                  accG = T(0);
+                  Gc = Gn;
+                  gi = min(gi + 1, clen - 1);
+                }
+                else
+                  rowT = w * step_delta<OP>(F.v, Fn.v, Gc.v);
+              }
+              t = F.tn;
             }
-            if (advG)
+            T rowV = w * accF;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
             {
-              Gc = G2;
-              ++gi;
-              G2 = col[min(gi + 1, clen - 1)];
-              accG = T(0);
+              rowV += __shfl_xor_sync(FULL, rowV, o);
+              rowT += __shfl_xor_sync(FULL, rowT, o);
             }
-            t = tn;
+            if (lane == 0 && (rowV != T(0) || rowT != T(0))) red_add2(&B.grad[2 * (roff + k)], rowV, rowT);
+            F = Fn;
           }
-          if (live)
-          {
-            atomicAdd(&sgv[fi], w * accF);
-            atomicAdd(&cgrad[2 * (size_t)gi], w * accG);
-          }
-          __syncwarp();
-          for (uint32_t k = lane; k < rlen; k += 32)
-          {
-            const T gv = sgv[k], gt = sgt[k];
-            if (gv != T(0) || gt != T(0)) red_add2(&B.grad[2 * (roff + k)], gv, gt);
-          }
-          __syncwarp();
+          if (live) atomicAdd(&cgrad[2 * (size_t)gi], w * accG);
         }
       }
       __syncthreads();
@@ -529,8 +541,20 @@ namespace sbg
     constexpr int SIDE = 0;
 #endif
     constexpr bool SQ = SIDE != 0;
-    // per-warp row-gradient buffers (none when only columns take gradients)
-    const size_t grad_per_warp = SIDE == 2 ? 0 : (size_t)lmax * 2 * sizeof(T);
+#ifdef SBG_BWD_WARP_ITEMS
+    constexpr bool WI = true;
+#else
+    constexpr bool WI = false;
+#endif
+#if !defined(SBG_BWD_LEGACY)
+    // the row-synchronous walk (no shared memory) unless an alternative is asked for
+    constexpr bool ROWSYNC = SIDE == 0 && !WI && !defined_stage_columns();
+#else
+    constexpr bool ROWSYNC = false;
+#endif
+    // per-warp row-gradient buffers (none when only columns take gradients,
+    // nor in the row-synchronous walk)
+    const size_t grad_per_warp = (SIDE == 2 || ROWSYNC) ? 0 : (size_t)lmax * 2 * sizeof(T);
     const size_t cols_bytes = (size_t)32 * lmax * sizeof(Elem<T>);
     const size_t budget = dev.smem_optin > 2048 ? dev.smem_optin - 2048 : 0;
 #if defined(SBG_BWD_STAGE_COLUMNS) && !defined(SBG_BWD_WARP_ITEMS)
@@ -554,11 +578,6 @@ namespace sbg
     // SBG_BWD_SQUARE_COLUMNS.
     // Per-warp items measured slower (58 against 50 ms): the column atomics
     // were not colliding; they stay available behind SBG_BWD_WARP_ITEMS.
-#ifdef SBG_BWD_WARP_ITEMS
-    constexpr bool WI = true;
-#else
-    constexpr bool WI = false;
-#endif
     const uint64_t G = ceil_div_u64(n, 32);
     auto items = [&](uint32_t qq) { return SQ ? ceil_div_u64(n, 32ull * qq) * G : tri_item_count(0, n, qq, G); };
     const uint64_t want_items = (uint64_t)dev.sms * (WI ? warps * 4 : 6);
@@ -570,21 +589,16 @@ namespace sbg
     SBG_CUDA(cudaMemsetAsync(queue, 0, 8, st));
     if (B.total_items > 0)
     {
-#if !defined(SBG_BWD_LEGACY)
-      // the lean step (same walk and arithmetic) unless an alternative is asked for
-      constexpr bool LEAN = SIDE == 0 && !WI && !defined_stage_columns();
-#else
-      constexpr bool LEAN = false;
-#endif
       void (*fn)(const BwdParams<T>) =
-          LEAN ? (bop == BWD_INNER ? pairs_backward_lean_kernel<T, BWD_INNER>
-                  : bop == BWD_L2DIST ? pairs_backward_lean_kernel<T, BWD_L2DIST>
-                                      : pairs_backward_lean_kernel<T, BWD_L1DIST>)
+          ROWSYNC ? (bop == BWD_INNER ? pairs_backward_rowsync_kernel<T, BWD_INNER>
+                  : bop == BWD_L2DIST ? pairs_backward_rowsync_kernel<T, BWD_L2DIST>
+                                      : pairs_backward_rowsync_kernel<T, BWD_L1DIST>)
                : (bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SIDE, WI>
                   : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SIDE, WI>
                                       : pairs_backward_kernel<T, BWD_L1DIST, SIDE, WI>);
       SBG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms);
+      const int per_sm = ROWSYNC ? ctas_per_sm(dev, warps, 0) : 1;
+      const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms * per_sm);
       fn<<<grid, warps * 32, smem, st>>>(B);
       SBG_CUDA(launched());
     }

@@ -202,7 +202,7 @@ extern "C"
     return guarded([&] {
       if (warps < 0 || warps > 32) throw Error(ST_INVALID_ARGUMENT, "warps must be in [0, 32]");
       if (row_chunk < 0 || row_chunk > 1024) throw Error(ST_INVALID_ARGUMENT, "row_chunk must be in [0, 1024]");
-      if (variant < 0 || variant > 6) throw Error(ST_INVALID_ARGUMENT, "variant must be in [0, 6]");
+      if (variant < 0 || variant > 8) throw Error(ST_INVALID_ARGUMENT, "variant must be in [0, 8]");
       if (order < 0 || order > 2) throw Error(ST_INVALID_ARGUMENT, "order must be 0, 1 or 2");
       settings().warps.store(warps);
       settings().rowChunk.store(row_chunk);
@@ -466,14 +466,17 @@ extern "C"
 
 namespace
 {
-  // Restores the process-wide (warps, rows per item) settings on scope exit.
+  // Restores the process-wide (warps, rows per item, window cap) settings on
+  // scope exit.
   struct ShapeOverride
   {
     int warps = sbg::settings().warps.load(), chunk = sbg::settings().rowChunk.load();
+    int cap = sbg::settings().windowCap.load();
     ~ShapeOverride()
     {
       sbg::settings().warps.store(warps);
       sbg::settings().rowChunk.store(chunk);
+      sbg::settings().windowCap.store(cap);
     }
   };
 
@@ -487,7 +490,7 @@ namespace
     const uint64_t nc = skip_mode == SBG_SKIP_NONE ? c->n : r.n;
     LengthStats ls;
     ls.lmax = max_points; ls.lmin = 1; ls.mean = max_points;
-    const Plan base = make_plan<T>(skip_mode, r.n, nc, ls, ls, dev, -1);
+    const Plan base = sbg::make_plan<T>(skip_mode, r.n, nc, ls, ls, dev, -1);
     std::vector<std::pair<int, int>> cands;
     for (int w : {16, 24, 32})
       for (uint32_t q : {base.q / 4, base.q / 2, base.q, base.q * 2})
@@ -501,6 +504,9 @@ namespace
       ~Events() { cudaEventDestroy(a); cudaEventDestroy(b); }
     } ev{e0, e1};
     ShapeOverride restore;
+    // the time-windowed kernel's window cap stays the default plan's while the
+    // shapes are timed: that is the cap a cached shape runs with
+    if (base.kvar == 6 && settings().windowCap.load() == 0) settings().windowCap.store((int)base.win_r);
     double best = 1e300;
     int bw = base.warps, bq = (int)base.q;
     for (const auto& cand : cands)
@@ -586,6 +592,20 @@ extern "C"
                  ? 1 : 0;
       if (warps) *warps = *hit ? w : 0;
       if (rows_per_item) *rows_per_item = *hit ? 32 * q : 0;
+    });
+  }
+
+  int sbg_tuning_cache_store(int dtype, int op, double p, int skip_mode, uint64_t n_rows, uint32_t max_points,
+                             int warps, int rows_per_item)
+  {
+    using namespace sbg;
+    return guarded([&] {
+      check_common(dtype, op, p, skip_mode);
+      if (warps < 1 || warps > 32) throw Error(ST_INVALID_ARGUMENT, "warps must be in [1, 32]");
+      if (rows_per_item < 32 || rows_per_item > 1024 || rows_per_item % 32)
+        throw Error(ST_INVALID_ARGUMENT, "rows_per_item must be a multiple of 32 in [32, 1024]");
+      tune_cache_put(tune_key(dtype == SBG_F32 ? 4 : 8, op_kind(op, p), skip_mode, n_rows, max_points), warps,
+                     rows_per_item / 32);
     });
   }
 

@@ -374,6 +374,39 @@ namespace sbg
       pl.row_cap = row_cap;
       pl.smem_bytes = smem_for(warps);
     }
+    else if (variant == 7 || variant == 8)
+    {
+      // the float32 measurement variants (pair_variants.cu); never automatic
+      if (sizeof(T) != 4) throw Error(ST_INVALID_ARGUMENT, "variants 7 and 8 are float32 only");
+      pl.smem = true;
+      pl.packed = false;
+      pl.kvar = variant;
+      size_t fixed, per_warp;
+      if (variant == 7)
+      {
+        pl.lmax_c = lmax_c;
+        pl.row_cap = lmax_r + (uint32_t)U;                   // the row, then U sentinel elements
+        fixed = (size_t)32 * lmax_c * es;                     // 32 columns, 8 bytes per element
+        per_warp = (size_t)pl.row_cap * 16 * es;              // 16 copies of every row element
+      }
+      else
+      {
+        pl.lmax_c = (uint32_t)padded_words((int)lmax_c - 1) + 1;  // padded column stride (words)
+        pl.row_cap = (uint32_t)padded_words((int)lmax_r - 1) + 1;
+        fixed = (size_t)2 * 32 * pl.lmax_c * sizeof(T);
+        per_warp = (size_t)2 * pl.row_cap * sizeof(T);
+      }
+      int w = 0;
+      for (int cand : {32, 24, 20, 16, 12, 8, 4})
+      {
+        if (want_w > 0 && cand > want_w) continue;
+        if (fixed + (size_t)cand * per_warp <= usable) { w = cand; break; }
+      }
+      if (w == 0) throw Error(ST_INVALID_ARGUMENT, "variant " + std::to_string(variant) +
+                                                       ": the PCFs do not fit in shared memory");
+      pl.warps = w;
+      pl.smem_bytes = fixed + (size_t)w * per_warp;
+    }
     else if (variant == 2)
     {
       pl.smem = false;

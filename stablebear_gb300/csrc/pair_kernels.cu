@@ -1040,6 +1040,11 @@ namespace sbg
                            size_t smem_bytes, cudaStream_t s)
   {
     dim3 g((unsigned)grid), b((unsigned)(warps * 32));
+    if (variant == 7 || variant == 8)
+    {
+      if constexpr (sizeof(T) == 4) return launch_pair_variant(L, opk, variant, warps, grid, smem_bytes, s);
+      else return cudaErrorInvalidValue;  // float32 only (the planner rejects double first)
+    }
     if (variant == 6) return launch_window<T>(opk, g, b, smem_bytes, s, L);
     if (variant == 1) return launch_op<T, 1>(opk, g, b, smem_bytes, s, L);
     if (variant == 2) return launch_op<T, 2>(opk, g, b, smem_bytes, s, L);

@@ -156,8 +156,14 @@ namespace sbg
     double mean = 0.0;
   };
 
-  template <typename T>
+  // The float32 measurement variants 7 (replicated row, one unified load per
+  // step) and 8 (merge path, one pair per warp), pair_variants.cu.
+  cudaError_t launch_pair_variant(const LaunchParams<float>& L, int opk, int variant, int warps, int grid,
+                                  size_t smem, cudaStream_t s);
+  int padded_words(int k);  // k + k / 32: variant 8's padded index
+
   // opk: the operation kind, for the launch-shape cache (-1: no lookup).
+  template <typename T>
   Plan make_plan(int mode, uint64_t n_rows, uint64_t n_cols, const LengthStats& rows, const LengthStats& cols,
                  const DeviceInfo& dev, int opk);
 

@@ -53,8 +53,11 @@ def set_tuning(warps: int = 0, row_chunk: int = 0, variant: int = 0, order: int 
     """Engine knobs (0 = automatic): warps per CTA, rows per work item / 32,
     kernel variant (1 shared-memory, 2 global-memory, 3 shared-memory two-load
     walk, 4 hybrid, 5 shared-memory with row times and values apart, 6
-    time-windowed shared memory), PCF order (1 as given, 2 sorted by
-    breakpoint count), output bytes per pipeline band."""
+    time-windowed shared memory; the float32 measurement variants 7, one
+    unified shared-memory load per step from a row replicated 16 times, and
+    8, merge path with one pair per warp, which the planner never picks),
+    PCF order (1 as given, 2 sorted by breakpoint count), output bytes per
+    pipeline band."""
     nat.check(nat.lib().sbg_set_tuning(int(warps), int(row_chunk), int(variant), int(order), int(band_bytes)))
 
 

@@ -2,10 +2,11 @@
 
 The autotuner times (warps per CTA, rows per work item) shapes on the real
 problem and caches the fastest under (element type, operation, skip mode,
-shape bucket).  Neither knob changes a result bit, so the test checks that a
-cached shape is found again and used, and that every shape it tried gives
-the same bits as the default plan, for the plain shared-memory kernel and
-the time-windowed one.
+shape bucket).  Neither knob changes a result bit (the time-windowed kernel
+keeps the default plan's window cap under a cached shape), so the test
+checks that a cached shape is found again and used, and that shapes pinned
+in the cache give the same bits as the default plan, for the plain
+shared-memory kernel and the time-windowed one.
 """
 import ctypes
 
@@ -74,13 +75,10 @@ def test_autotune_caches_a_shape_and_keeps_every_bit(env, kind):
     assert hit.value == 0
     # the default call now plans with the cached shape: same bits
     np.testing.assert_array_equal(_run(torch, nat, dp, do, n, lmax, out), default)
-    # and every forced shape gives the same bits
-    for warps, q in ((16, 1), (32, 2), (24, 4)):
-        nat.check(lib.sbg_set_tuning(warps, q, 0, 0, 0))
-        try:
-            np.testing.assert_array_equal(_run(torch, nat, dp, do, n, lmax, out), default)
-        finally:
-            nat.check(lib.sbg_set_tuning(0, 0, 0, 0, 0))
+    # and so does every other shape pinned in the cache for this key
+    for warps, rows in ((16, 32), (32, 64), (24, 128), (32, 1024)):
+        nat.check(lib.sbg_tuning_cache_store(nat.F32, 0, 1.0, nat.SKIP_LOWER_NODIAG, n, lmax, warps, rows))
+        np.testing.assert_array_equal(_run(torch, nat, dp, do, n, lmax, out), default)
     nat.check(lib.sbg_tuning_cache_clear())
     nat.check(lib.sbg_tuning_cache_lookup(nat.F32, 0, 1.0, nat.SKIP_LOWER_NODIAG, n, lmax, ctypes.byref(w),
                                           ctypes.byref(r), ctypes.byref(hit)))

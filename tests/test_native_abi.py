@@ -181,7 +181,8 @@ def test_settings_roundtrip(lib):
     sb.set_tuning()
     # the time-windowed variant and its window cap
     assert lib.sbg_set_tuning(0, 0, 6, 0, 0) == 0
-    assert lib.sbg_set_tuning(0, 0, 7, 0, 0) == -1
+    assert lib.sbg_set_tuning(0, 0, 8, 0, 0) == 0  # the measurement variants 7 and 8
+    assert lib.sbg_set_tuning(0, 0, 9, 0, 0) == -1
     assert b"variant" in lib.sbg_last_error()
     sb.set_window_cap(40)
     assert sb.get_window_cap() == 40
