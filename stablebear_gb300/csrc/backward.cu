@@ -430,6 +430,171 @@ namespace sbg
     }
   }
 
+  // The default backward: the row walked in windows of W elements.  The
+  // row-synchronous walk above waits, at every row element, for the lane
+  // with the most column breakpoints before the next row breakpoint (about
+  // 5 for a mean of 1 on the fwd + bwd workload).  Here the lanes walk
+  // freely through W row elements at a time, with the walk's own step (ties
+  // go to the row; a zero-width column step gets no time gradient), and a
+  // lane that leaves row element k stores its value- and time-gradient terms
+  // for k in its own slot of a per-warp [W][32] shared array: a plain store,
+  // no atomics, no bank conflicts (lane l's slot is at bank pair l % 16).
+  // When every lane has left the window's last element, the 32 slots of each
+  // element are summed (two lanes per element, a skewed read order) and
+  // added to global memory once.  Lanes with no weight take no part and
+  // leave zeros in their slots.  Column gradients leave as in the walks
+  // above.
+  template <typename T, int OP, int W>
+  __global__ void __launch_bounds__(512) pairs_backward_window_kernel(const __grid_constant__ BwdParams<T> B)
+  {
+    static_assert(W >= 1 && W <= 16, "two lanes per window element");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ unsigned long long s_item;
+    __shared__ unsigned int s_next_row;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const unsigned FULL = 0xffffffffu;
+    // slot (element j of the window, lane l) at [j * 32 + l]: (value-gradient term, time-gradient term)
+    Elem<T>* slots = reinterpret_cast<Elem<T>*>(smem_raw) + (size_t)warp * W * 32;
+
+    for (;;)
+    {
+      if (threadIdx.x == 0)
+      {
+        s_item = atomicAdd(B.queue, 1ull);
+        s_next_row = 0;
+      }
+      __syncthreads();
+      const unsigned long long item = s_item;
+      if (item >= B.total_items) break;
+      const uint64_t G = ceil_div_u64(B.n, 32);
+      uint64_t c, g;
+      tri_decode(item, 0, B.n, B.q, G, &c, &g);
+      uint64_t row_lo = c * 32ull * B.q;
+      uint64_t row_hi = row_lo + 32ull * B.q;
+      if (row_hi > B.n) row_hi = B.n;
+      const uint64_t col0 = 32ull * g;
+      if (row_lo < col0 + 1) row_lo = col0 + 1;  // the diagonal is handled by diag_backward_kernel
+
+      const uint64_t cj = col0 + lane;
+      const bool cvalid = cj < B.n;
+      uint64_t corig = B.perm ? B.perm[cvalid ? cj : col0] : (cvalid ? cj : col0);
+      if (corig >= B.n) corig = 0;  // never expected: the order is a permutation
+      const uint64_t coff = B.off[corig];
+      const uint32_t clen = (uint32_t)(B.off[corig + 1] - coff);
+      const uint32_t maxlc = __reduce_max_sync(FULL, clen);  // warp-uniform: bounds the walk below
+      const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > B.npts);
+      if (item_ok)
+      {
+        const Elem<T>* col = B.pk + coff;
+        T* cgrad = B.grad + 2 * coff;
+        for (;;)
+        {
+          unsigned r = 0;
+          if (lane == 0) r = atomicAdd(&s_next_row, 1u);
+          r = __shfl_sync(FULL, r, 0);
+          const uint64_t i = row_lo + r;
+          if (i >= row_hi) break;
+          const uint64_t iorig = B.perm ? B.perm[i] : i;
+          if (iorig >= B.n) continue;  // never expected: the order is a permutation
+          const uint64_t roff = B.off[iorig];
+          const uint32_t rlen = (uint32_t)(B.off[iorig + 1] - roff);
+          if (rlen == 0 || roff + rlen > B.npts) continue;
+          T w = T(0);
+          if (cvalid && cj < i)
+          {
+            const uint64_t idx = condensed_index(B.mode, iorig, corig);
+            w = B.grad_out[idx];
+            if (OP == BWD_L2DIST)
+            {
+              const T D = B.fwd[idx];
+              w = D > T(0) ? w / D : T(0);
+            }
+          }
+          const bool live = w != T(0);
+          if (!__any_sync(FULL, live)) continue;
+          if (!live)
+            for (int j = 0; j < W; ++j) slots[j * 32 + lane] = Elem<T>{T(0), T(0)};
+
+          const Elem<T>* row = B.pk + roff;
+          Elem<T> F = row[0], F2 = row[rlen > 1 ? 1 : 0];
+          Elem<T> Gc = col[0], G2 = col[clen > 1 ? 1 : 0];
+          uint32_t fi = 0, gi = 0;
+          T t = T(0), accF = T(0), accG = T(0);
+          for (uint32_t kb = 0; kb < rlen; kb += W)
+          {
+            const uint32_t ke = min(kb + (uint32_t)W, rlen);
+            // Walk until this lane has left row element ke - 1 (for the last
+            // element: taken the last rectangle, to TMAX).  A lane takes at
+            // most W row steps and clen - 1 column steps in a window, so the
+            // bound W + maxlc ends the loop whatever the data; it is the same
+            // in every lane, so all 32 lanes run every iteration's vote.
+            for (uint32_t guard = 0; guard <= (uint32_t)W + maxlc; ++guard)
+            {
+              const bool act = live && fi < ke;
+              if (!__any_sync(FULL, act)) break;
+              if (act)
+              {
+                const bool takeF = row_first(F.tn, Gc.tn);
+                const T tn = takeF ? F.tn : Gc.tn;
+                const T dt = tn - t;
+                T cf, cg;
+                seg_coeffs<OP>(F.v, Gc.v, cf, cg);
+                accF = fma(dt, cf, accF);
+                accG = fma(dt, cg, accG);
+                if (takeF)
+                {
+                  // leave row element fi; a breakpoint shared with the
+                  // column, or the row's end, has no time gradient
+                  const T dF = (F.tn == Gc.tn || fi + 1 >= rlen) ? T(0) : w * step_delta<OP>(F.v, F2.v, Gc.v);
+                  slots[(fi - kb) * 32 + lane] = Elem<T>{w * accF, dF};
+                  accF = T(0);
+                  F = F2;
+                  ++fi;
+                  F2 = row[min(fi + 1, rlen - 1)];
+                }
+                else
+                {
+                  // Gc.tn < F.tn <= TMAX: the column has a next element, G2
+                  const T dG = (dt == T(0)) ? T(0) : w * step_delta<OP>(Gc.v, G2.v, F.v);
+                  red_add2(&cgrad[2 * (size_t)gi], w * accG, dG);
+                  accG = T(0);
+                  Gc = G2;
+                  ++gi;
+                  G2 = col[min(gi + 1, clen - 1)];
+                }
+                t = tn;
+              }
+            }
+            __syncwarp();
+            // element j of the window: lanes j and j + 16 each sum 16 of its
+            // 32 slots, in an order skewed by j so that the lanes of a
+            // half-warp read 16 different bank pairs
+            const uint32_t nel = ke - kb;
+            const uint32_t j = lane & 15, h = lane >> 4;
+            T sv = T(0), st = T(0);
+            if (j < nel)
+            {
+#pragma unroll
+              for (int m = 0; m < 16; ++m)
+              {
+                const Elem<T> s = slots[j * 32 + h * 16 + ((m + j) & 15)];
+                sv += s.v;
+                st += s.tn;
+              }
+            }
+            sv += __shfl_xor_sync(FULL, sv, 16);
+            st += __shfl_xor_sync(FULL, st, 16);
+            if (h == 0 && j < nel && (sv != T(0) || st != T(0))) red_add2(&B.grad[2 * (roff + kb + j)], sv, st);
+            __syncwarp();
+          }
+          if (live) atomicAdd(&cgrad[2 * (size_t)gi], w * accG);
+        }
+      }
+      __syncthreads();
+    }
+  }
+
   // (dL/dv_k, dL/dt_{k+1}) slots to the point layout (dL/dt_k, dL/dv_k).
   // The slot of a PCF's last element holds no time gradient (there is no
   // breakpoint after it).  One warp per PCF.
@@ -546,15 +711,22 @@ namespace sbg
 #else
     constexpr bool WI = false;
 #endif
-#if !defined(SBG_BWD_LEGACY)
-    // the row-synchronous walk (no shared memory) unless an alternative is asked for
-    constexpr bool ROWSYNC = SIDE == 0 && !WI && !defined_stage_columns();
+    // The walk in windows of row elements (the default), the row-synchronous
+    // walk (SBG_BWD_ROWSYNC) or the free-running walk with per-warp
+    // row-gradient buffers (SBG_BWD_LEGACY and the alternatives above).
+#if defined(SBG_BWD_LEGACY)
+    constexpr int WALK = 0;
+#elif defined(SBG_BWD_ROWSYNC)
+    constexpr int WALK = 1;
 #else
-    constexpr bool ROWSYNC = false;
+    constexpr int WALK = 2;
 #endif
+    constexpr bool ROWSYNC = WALK == 1 && SIDE == 0 && !WI && !defined_stage_columns();
+    constexpr bool WINDOWED = WALK == 2 && SIDE == 0 && !WI && !defined_stage_columns();
+    constexpr int BWD_W = 8;  // row elements per window
     // per-warp row-gradient buffers (none when only columns take gradients,
-    // nor in the row-synchronous walk)
-    const size_t grad_per_warp = (SIDE == 2 || ROWSYNC) ? 0 : (size_t)lmax * 2 * sizeof(T);
+    // nor in the row-synchronous and windowed walks)
+    const size_t grad_per_warp = (SIDE == 2 || ROWSYNC || WINDOWED) ? 0 : (size_t)lmax * 2 * sizeof(T);
     const size_t cols_bytes = (size_t)32 * lmax * sizeof(Elem<T>);
     const size_t budget = dev.smem_optin > 2048 ? dev.smem_optin - 2048 : 0;
 #if defined(SBG_BWD_STAGE_COLUMNS) && !defined(SBG_BWD_WARP_ITEMS)
@@ -564,10 +736,12 @@ namespace sbg
 #endif
     B.cols_cap = stage ? lmax : 0;
     const size_t fixed = stage ? cols_bytes : 0;
-    int warps = 32;
+    int warps = WINDOWED ? 16 : 32;
     while (warps > 1 && fixed + (size_t)warps * grad_per_warp > budget) warps /= 2;
     if (stage) while (warps < 32 && fixed + (size_t)(warps + 8) * grad_per_warp <= budget) warps += 8;
-    const size_t smem = fixed + (size_t)warps * grad_per_warp;
+    // the windowed walk: one [BWD_W][32] slot array per warp
+    const size_t smem =
+        WINDOWED ? (size_t)warps * BWD_W * 32 * sizeof(Elem<T>) : fixed + (size_t)warps * grad_per_warp;
     if (smem > budget) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
     // The ordered-pairs variants measured slower on GB300 (N = 4096, L2
     // kernel): rows only, forward + backward 74 ms against 46 ms at the time
@@ -590,14 +764,20 @@ namespace sbg
     if (B.total_items > 0)
     {
       void (*fn)(const BwdParams<T>) =
-          ROWSYNC ? (bop == BWD_INNER ? pairs_backward_rowsync_kernel<T, BWD_INNER>
-                  : bop == BWD_L2DIST ? pairs_backward_rowsync_kernel<T, BWD_L2DIST>
-                                      : pairs_backward_rowsync_kernel<T, BWD_L1DIST>)
-               : (bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SIDE, WI>
-                  : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SIDE, WI>
-                                      : pairs_backward_kernel<T, BWD_L1DIST, SIDE, WI>);
+          WINDOWED ? (bop == BWD_INNER ? pairs_backward_window_kernel<T, BWD_INNER, BWD_W>
+                      : bop == BWD_L2DIST ? pairs_backward_window_kernel<T, BWD_L2DIST, BWD_W>
+                                          : pairs_backward_window_kernel<T, BWD_L1DIST, BWD_W>)
+          : ROWSYNC ? (bop == BWD_INNER ? pairs_backward_rowsync_kernel<T, BWD_INNER>
+                       : bop == BWD_L2DIST ? pairs_backward_rowsync_kernel<T, BWD_L2DIST>
+                                           : pairs_backward_rowsync_kernel<T, BWD_L1DIST>)
+                    : (bop == BWD_INNER ? pairs_backward_kernel<T, BWD_INNER, SIDE, WI>
+                       : bop == BWD_L2DIST ? pairs_backward_kernel<T, BWD_L2DIST, SIDE, WI>
+                                           : pairs_backward_kernel<T, BWD_L1DIST, SIDE, WI>);
       SBG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      const int per_sm = ROWSYNC ? ctas_per_sm(dev, warps, 0) : 1;
+      // persistent CTAs: as many per SM as registers, threads and shared memory allow
+      int per_sm = 1;
+      SBG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, warps * 32, smem));
+      per_sm = std::max(1, per_sm);
       const unsigned grid = (unsigned)std::min<uint64_t>(B.total_items, (uint64_t)dev.sms * per_sm);
       fn<<<grid, warps * 32, smem, st>>>(B);
       SBG_CUDA(launched());
