@@ -723,7 +723,10 @@ namespace sbg
 #endif
     constexpr bool ROWSYNC = WALK == 1 && SIDE == 0 && !WI && !defined_stage_columns();
     constexpr bool WINDOWED = WALK == 2 && SIDE == 0 && !WI && !defined_stage_columns();
-    constexpr int BWD_W = 8;  // row elements per window
+#ifndef SBG_BWD_WINDOW
+#define SBG_BWD_WINDOW 8
+#endif
+    constexpr int BWD_W = SBG_BWD_WINDOW;  // row elements per window
     // per-warp row-gradient buffers (none when only columns take gradients,
     // nor in the row-synchronous and windowed walks)
     const size_t grad_per_warp = (SIDE == 2 || ROWSYNC || WINDOWED) ? 0 : (size_t)lmax * 2 * sizeof(T);
