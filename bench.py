@@ -102,8 +102,8 @@ def _traffic_per_launch(kernel, n):
 
 
 def _hbm_peak():
-    """HBM copy bandwidth (GB/s) measured on the GB300s, else the
-    earlier single measurement."""
+    """HBM copy bandwidth (GB/s) from the measured-peaks file beside this
+    script, else one earlier GB300 measurement."""
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
     try:
         with open(path) as fh:
@@ -684,7 +684,7 @@ def main():
         best = max(CPU_BUILDS, key=lambda b: builds[b][0])
         rate, dt = builds[best][0], builds[best][1]
         # parity against the reference's algorithm without contraction (bit
-        # for bit the checker build the golden tests pin)
+        # for bit the oracle build that the golden tests pin)
         vals = builds["o3_off"][2]
         host = out.cpu().numpy() if pairs <= 6_000_000_000 else None
         got = np.concatenate([host[int(i) * (int(i) - 1) // 2: int(i) * (int(i) - 1) // 2 + int(i)] for i in rows])
