@@ -211,6 +211,23 @@ def run_aux(args):
                          "plain_loop_pairs_per_s": pairs / (ms_plain / 1e3), "speedup_vs_plain": ms_plain / ms_b,
                          "autotuned_ms": tuned, "launch": info, "max_rel_err_vs_reference_cpu": max(errs)}
             b.close()
+            # the same batch with the window cap among the tuned settings
+            bw = PairwiseBatch(probs, op=op, p=p, graph=True, tune_window=True)
+            bw.run()
+            torch.cuda.synchronize()
+            tuned_w = bw.autotune()
+            ms_w = _time_device(bw.run, max(3, args.steps), 2)
+            bw.run()
+            torch.cuda.synchronize()
+            errs_w = []
+            for k in (0, 255):
+                pp, oo = probs[k]
+                want = orc.evaluate(pp, oo, op=orc.OP_L1 if op == "l1" else orc.OP_LP, p=p, threads=threads)
+                got = bw.outputs[k].cpu().numpy()
+                errs_w.append(float(np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-30))))
+            rep[name]["tune_window"] = {"batched_ms": ms_w, "autotuned_ms": tuned_w, "launch": bw.info(),
+                                        "max_rel_err_vs_reference_cpu": max(errs_w)}
+            bw.close()
         rep.update({"workload": "512 problems, N_i~U{50..2000}, L~U{8..1024}, f32 Betti-like", "pairs": pairs,
                     "segments": segs})
     elif args.config == "fwdbwd":

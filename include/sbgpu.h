@@ -249,6 +249,7 @@ typedef struct sbg_problem {
 typedef struct sbg_batch sbg_batch;
 #define SBG_BATCH_GRAPH 1         /* launch through a captured CUDA graph */
 #define SBG_BATCH_CALLER_ORDER 2  /* keep the caller's PCF order (default: sorted by breakpoint count) */
+#define SBG_BATCH_TUNE_WINDOW 4   /* let sbg_batch_autotune move the time-windowed kernel's window cap */
 
 /* Builds the batch: length orders, packed layouts, descriptors ordered by
  * estimated merge work (largest first).  Synchronises the device once. */
@@ -257,10 +258,19 @@ int sbg_batch_create(int dtype, int op, double p, int skip_mode, const sbg_probl
 /* Computes every problem of the batch on `stream` (queue reset + one kernel;
  * graph replay when created with SBG_BATCH_GRAPH). */
 int sbg_batch_launch(sbg_batch* batch, void* stream);
-/* Times (warps per CTA, rows per work item) settings on this batch, keeps the
- * fastest; *best_ms receives its time per launch. */
+/* Times (warps per CTA, rows per work item) settings on this batch, then
+ * splits of shared memory between the column block and the row buffers,
+ * and keeps the fastest; *best_ms receives its time per launch.  The split
+ * is the hybrid kernel's column block (f64, or variant 4) and, only for a
+ * batch created with SBG_BATCH_TUNE_WINDOW, the time-windowed kernel's
+ * window cap.  Without that flag no tuned setting changes a bit of a
+ * result; with it, window ends move with the cap, so sums may change in
+ * their last bits (within the kernel's stated accuracy). */
 int sbg_batch_autotune(sbg_batch* batch, void* stream, double* best_ms);
 int sbg_batch_info(const sbg_batch* batch, uint64_t* items, uint64_t* pairs, int* warps, int* rows_per_item);
+/* Elements per PCF held in the shared column block: the window cap of the
+ * time-windowed kernel, or the hybrid kernel's column block. */
+int sbg_batch_shared_split(const sbg_batch* batch, uint32_t* column_elements);
 void sbg_batch_destroy(sbg_batch* batch);
 
 /* ---- device entry that allocates nothing --------------------------------------

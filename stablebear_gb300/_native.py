@@ -34,6 +34,7 @@ I32, I64 = 2, 3  # integer PCFs (sbg_iterate_rectangles)
 OP_L1, OP_LP, OP_L2_INNER = 0, 1, 2
 SKIP_NONE, SKIP_LOWER_NODIAG, SKIP_LOWER = 0, 1, 2
 FLAG_ASYMMETRIC, FLAG_DIAGONAL, FLAG_NEGATIVE = 1, 2, 4  # sbg_dense_to_condensed_device
+BATCH_GRAPH, BATCH_CALLER_ORDER, BATCH_TUNE_WINDOW = 1, 2, 4  # sbg_batch_create flags
 
 # Every symbol include/sbgpu.h declares, with (restype, argtypes).
 _P = ctypes.c_void_p
@@ -80,6 +81,7 @@ SIGNATURES = {
     "sbg_batch_launch": (_I, [_P, _P]),
     "sbg_batch_autotune": (_I, [_P, _P, ctypes.POINTER(_D)]),
     "sbg_batch_info": (_I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "sbg_batch_shared_split": (_I, [_P, ctypes.POINTER(ctypes.c_uint32)]),
     "sbg_batch_destroy": (None, [_P]),
     "sbg_output_count": (_U64, [_I, _U64, _U64]),
     "sbg_kernel_launches": (_U64, []),

@@ -35,9 +35,13 @@ class PairwiseBatch:
     ``problems``: a list of ``(points, offsets)`` CSR pairs (numpy, host).
     ``run()`` computes all problems on the current CUDA stream and returns
     the device outputs (torch tensors in condensed order).
+    ``tune_window=True`` lets ``autotune()`` also move the time-windowed
+    kernel's window cap (the split of shared memory between the column
+    block and the row buffers); window ends then move, so sums may change in
+    their last bits.  Without it no tuned setting changes a result.
     """
 
-    def __init__(self, problems, op="l1", p=1.0, graph=True, caller_order=False, device=None):
+    def __init__(self, problems, op="l1", p=1.0, graph=True, caller_order=False, device=None, tune_window=False):
         import torch
         if op not in _OPS:
             raise ValueError(f"op must be one of {sorted(_OPS)}")
@@ -71,7 +75,8 @@ class PairwiseBatch:
             self.sizes.append(n)
             arr[k] = _Problem(dp.data_ptr(), do.data_ptr(), off.ctypes.data, n, out.data_ptr())
         h = ctypes.c_void_p()
-        flags = (1 if graph else 0) | (2 if caller_order else 0)
+        flags = ((nat.BATCH_GRAPH if graph else 0) | (nat.BATCH_CALLER_ORDER if caller_order else 0)
+                 | (nat.BATCH_TUNE_WINDOW if tune_window else 0))
         nat.check(nat.lib().sbg_batch_create(self.code, opc, self.p, skip, ctypes.cast(arr, ctypes.c_void_p),
                                              len(problems), flags, ctypes.byref(h)))
         self._h = h
@@ -94,7 +99,10 @@ class PairwiseBatch:
         warps, rows = ctypes.c_int(), ctypes.c_int()
         nat.check(nat.lib().sbg_batch_info(self._h, ctypes.byref(items), ctypes.byref(pairs), ctypes.byref(warps),
                                            ctypes.byref(rows)))
-        return {"items": items.value, "pairs": pairs.value, "warps": warps.value, "rows_per_item": rows.value}
+        split = ctypes.c_uint32()
+        nat.check(nat.lib().sbg_batch_shared_split(self._h, ctypes.byref(split)))
+        return {"items": items.value, "pairs": pairs.value, "warps": warps.value, "rows_per_item": rows.value,
+                "column_elements": split.value}
 
     def matrices(self):
         """The results as host ``DistanceMatrix`` / ``SymmetricMatrix``."""

@@ -12,8 +12,10 @@
 //   * a launch is one queue reset plus one kernel; with SBG_BATCH_GRAPH the
 //     pair is captured once into a CUDA graph and replayed;
 //   * sbg_batch_autotune times a few (warps per CTA, rows per item)
-//     settings on the real batch, then a few sizes of the shared column
-//     block, and keeps the fastest.
+//     settings on the real batch, then a few splits of shared memory between
+//     the column block and the row buffers (the hybrid kernel's column
+//     block; with SBG_BATCH_TUNE_WINDOW the time-windowed kernel's window
+//     cap), and keeps the fastest.
 #include "../../include/sbgpu.h"
 #include "sbg_internal.hpp"
 
@@ -31,6 +33,7 @@ namespace sbg
     virtual void launch(cudaStream_t st) = 0;
     virtual double autotune(cudaStream_t st) = 0;
     virtual void info(uint64_t* items, uint64_t* pairs, int* warps, int* rows_per_item) const = 0;
+    virtual uint32_t shared_split() const = 0;
   };
 
   template <typename T>
@@ -39,6 +42,7 @@ namespace sbg
     int op = 0, mode = 0, opk = 0;
     double p = 1.0;
     bool use_graph = false;
+    bool tune_window = false;   // the autotune may move the window cap (and so window ends)
     DeviceInfo dev;
     std::vector<ProblemDesc<T>> descs;   // host copy, in launch order
     std::vector<uint64_t> q_base;        // per launch-order problem: chosen q at scale 1
@@ -65,12 +69,18 @@ namespace sbg
 
     // Rows per item and warps; the time-windowed layout depends on both.
     // False (and nothing changed) when that layout does not fit.
+    uint64_t max_q(uint32_t qscale) const
+    {
+      uint64_t qmax = 1;
+      for (size_t k = 0; k < descs.size(); ++k) qmax = std::max<uint64_t>(qmax, q_base[k] * qscale);
+      return qmax;
+    }
+
     bool rebuild_items(uint32_t warps, uint32_t qscale)
     {
       if (windowed)
       {
-        uint64_t qmax = 1;
-        for (size_t k = 0; k < descs.size(); ++k) qmax = std::max<uint64_t>(qmax, q_base[k] * qscale);
+        const uint64_t qmax = max_q(qscale);
         Plan trial = pl;
         if (qmax > 1024 ||
             !window_layout(trial, sizeof(Elem<T>), (int)warps, (uint32_t)(32 * qmax), lmax, usable, win_cap))
@@ -175,7 +185,33 @@ namespace sbg
         }
       }
       if (!rebuild_items(bw, bs)) throw Error(ST_INTERNAL, "batch autotune: the chosen layout no longer fits");
-      if (windowed) return best;
+      if (windowed)
+      {
+        if (!tune_window) return best;
+        // Window caps from the largest that fits the chosen shape down to
+        // half the batch's cap: a smaller cap leaves fewer elements per
+        // window in the column block and row buffers (more windows per
+        // pair), a larger one only fits fewer warps or rows per item.
+        const uint32_t base = win_cap;
+        uint32_t most = base;
+        Plan probe;
+        const uint64_t qmax = max_q(bs);
+        if (qmax <= 1024 &&
+            window_layout(probe, sizeof(Elem<T>), (int)bw, (uint32_t)(32 * qmax), lmax, usable, 0))
+          most = std::max(most, probe.lmax_c);
+        uint32_t bc = base;
+        for (uint32_t c : {most, base * 3 / 4, base / 2})
+        {
+          if (c < 8 || c == base) continue;
+          win_cap = c;
+          if (!rebuild_items(bw, bs)) continue;
+          const double ms = time_once(st, 2);
+          if (ms < best) { best = ms; bc = c; }
+        }
+        win_cap = bc;
+        if (!rebuild_items(bw, bs)) throw Error(ST_INTERNAL, "batch autotune: the chosen window cap no longer fits");
+        return best;
+      }
       // Hybrid kernel: column groups longer than the staging block read
       // their columns through L1; a smaller block leaves more of the SM's
       // unified L1/shared memory to the rows, which are always read through L1.
@@ -206,6 +242,10 @@ namespace sbg
       if (warps) *warps = pl.warps;
       if (rows_per_item) *rows_per_item = (int)(32 * q_scale);
     }
+
+    // elements per PCF in the shared column block: the window cap of the
+    // time-windowed kernel, or the hybrid kernel's column block
+    uint32_t shared_split() const override { return pl.lmax_c; }
   };
 
   template <typename T>
@@ -214,6 +254,7 @@ namespace sbg
     std::unique_ptr<Batch<T>> b(new Batch<T>);
     b->op = op; b->p = p; b->mode = mode; b->opk = op_kind(op, p);
     b->use_graph = (flags & SBG_BATCH_GRAPH) != 0;
+    b->tune_window = (flags & SBG_BATCH_TUNE_WINDOW) != 0;
     b->dev = device_info();
     const bool sort_len = (flags & SBG_BATCH_CALLER_ORDER) == 0;
     // the time-windowed kernel for float (the hybrid one on request), the
@@ -414,6 +455,14 @@ extern "C"
     return guarded_batch([&] {
       if (!batch) throw sbg::Error(sbg::ST_INVALID_ARGUMENT, "null batch");
       batch->impl->info(items, pairs, warps, rows_per_item);
+    });
+  }
+
+  int sbg_batch_shared_split(const sbg_batch* batch, uint32_t* column_elements)
+  {
+    return guarded_batch([&] {
+      if (!batch || !column_elements) throw sbg::Error(sbg::ST_INVALID_ARGUMENT, "null pointer");
+      *column_elements = batch->impl->shared_split();
     });
   }
 

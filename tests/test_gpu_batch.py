@@ -159,3 +159,28 @@ def test_batch_f64_windowed_and_hybrid(variant):
             want = orc.evaluate(pts, off, op=orc.OP_L2, mode=orc.MODE_KERNEL, truth=True)
             assert rel_err(got, want, floor=1.0) <= 1e-12
     b.close()
+
+
+def test_batch_autotune_with_window_cap():
+    """With tune_window the autotune may move the window cap (the split of
+    shared memory between the column block and the row buffers): the
+    results stay within the float32 bound, and without the flag the cap the
+    batch was made with is kept."""
+    from stablebear_gb300.batch import PairwiseBatch
+    from oracle import oracle as orc
+    probs = _problems(11, 24, nmax=400, lmax=900)
+    fixed = PairwiseBatch(probs, op="l1", graph=False)
+    cap0 = fixed.info()["column_elements"]
+    fixed.autotune()
+    assert fixed.info()["column_elements"] == cap0
+    fixed.close()
+    b = PairwiseBatch(probs, op="l1", graph=True, tune_window=True)
+    assert b.info()["column_elements"] == cap0
+    assert b.autotune() > 0
+    cap = b.info()["column_elements"]
+    assert cap >= 8
+    outs = [o.cpu().numpy() for o in b.run()]
+    for (pts, off), got in zip(probs, outs):
+        if len(off) > 2:
+            assert rel_err(got, orc.evaluate(pts, off)) <= 1e-5
+    b.close()
