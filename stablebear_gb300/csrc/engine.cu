@@ -14,6 +14,7 @@
 #include "host_copy.hpp"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <map>
@@ -561,21 +562,6 @@ namespace sbg
     return s;
   }
 
-  // The host version of the windowed length order (sort.cu); both give the
-  // same permutation.
-  static std::vector<uint32_t> length_order(const uint64_t* off, uint64_t n)
-  {
-    std::vector<uint32_t> perm(n);
-    std::iota(perm.begin(), perm.end(), 0u);
-    auto len = [off](uint32_t a) { return std::min<uint64_t>(off[a + 1] - off[a], 0xffffffffull); };
-    for (uint64_t w0 = 0; w0 < n; w0 += LENGTH_ORDER_WINDOW)
-    {
-      const uint64_t w1 = std::min<uint64_t>(n, w0 + LENGTH_ORDER_WINDOW);
-      std::stable_sort(perm.begin() + w0, perm.begin() + w1,
-                       [&len](uint32_t a, uint32_t b) { return len(a) < len(b); });
-    }
-    return perm;
-  }
 
   // ---- device entry -------------------------------------------------------------
 
@@ -844,6 +830,32 @@ namespace sbg
 
   namespace
   {
+    // With the device-verbose setting on, the host entry reports on stderr
+    // when each of its phases ended (host clock, ms since the call began);
+    // declared first in the call, it reports last, after the buffers are
+    // freed.
+    struct PhaseLog
+    {
+      bool on = settings().deviceVerbose.load();
+      std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+      std::string text;
+      void mark(const char* what, long k = -1)
+      {
+        if (!on) return;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        char buf[64];
+        if (k >= 0) std::snprintf(buf, sizeof buf, " %s%ld %.1f", what, k, ms);
+        else std::snprintf(buf, sizeof buf, " %s %.1f", what, ms);
+        text += buf;
+      }
+      ~PhaseLog()
+      {
+        if (!on) return;
+        mark("freed");
+        std::fprintf(stderr, "sbgpu host entry, ms since start:%s\n", text.c_str());
+      }
+    };
+
     struct StreamGuard
     {
       cudaStream_t s = nullptr;
@@ -880,6 +892,7 @@ namespace sbg
   void compute_host(int mode, int op, double p, const PcfSet<T>& rows, const PcfSet<T>* cols, T* out, bool validate,
                     const RunControl& ctl)
   {
+    PhaseLog phases;
     if (mode == MODE_CROSS && !cols) throw Error(ST_INVALID_ARGUMENT, "cdist needs a column set");
     const PcfSet<T>& cs = (mode == MODE_CROSS) ? *cols : rows;
     if (validate)
@@ -887,6 +900,7 @@ namespace sbg
       validate_pcfs(rows, mode == MODE_CROSS ? "X" : "input");
       if (mode == MODE_CROSS) validate_pcfs(cs, "Y");
     }
+    phases.mark("checked");
     (void)op_kind(op, p);
     const uint64_t total = output_count(mode, rows.n, cs.n);
     if (total == 0) return;
@@ -901,6 +915,7 @@ namespace sbg
     DeviceSet<T> drows, dcols;
     drows.upload(rows, compute.s);
     if (mode == MODE_CROSS) dcols.upload(cs, compute.s);
+    phases.mark("uploaded");
 
     // Processing order: by length within windows (unless the order setting
     // asks for the caller's), the permutation the device entry computes on
@@ -910,28 +925,23 @@ namespace sbg
     const size_t out_bytes = (size_t)total * sizeof(T);
     const size_t budget = (size_t)((double)freeb * 0.8);
     int order = settings().order.load();
-    std::vector<uint32_t> rperm, cperm;
-    bool sorted = false;
-    if (order != 1 && rows.n <= 0xffffffffull && cs.n <= 0xffffffffull)
-    {
-      sorted = true;
-      cperm = length_order(cs.off, cs.n);
-      rperm = (mode == MODE_CROSS) ? length_order(rows.off, rows.n) : cperm;
-    }
+    const bool sorted = order != 1 && rows.n <= 0xffffffffull && cs.n <= 0xffffffffull;
     DeviceBuffer drperm, dcperm;
     if (sorted)
     {
-      drperm.reset(rperm.size() * sizeof(uint32_t));
-      SBG_CUDA(cudaMemcpyAsync(drperm.get(), rperm.data(), rperm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, compute.s));
+      // computed on the stream from the uploaded offsets (one launch)
+      drperm.reset(std::max<uint64_t>(1, rows.n) * sizeof(uint32_t));
+      length_order_device(drows.view.off, rows.n, drperm.as<uint32_t>(), nullptr, compute.s);
       if (mode == MODE_CROSS)
       {
-        dcperm.reset(cperm.size() * sizeof(uint32_t));
-        SBG_CUDA(cudaMemcpyAsync(dcperm.get(), cperm.data(), cperm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, compute.s));
+        dcperm.reset(std::max<uint64_t>(1, cs.n) * sizeof(uint32_t));
+        length_order_device(dcols.view.off, cs.n, dcperm.as<uint32_t>(), nullptr, compute.s);
       }
     }
 
     const Plan pl = make_plan<T>(mode, rows.n, cs.n, rstat, cstat, dev, op_kind(op, p));
     const uint64_t chunk_rows = 32ull * pl.q;
+    phases.mark("ordered");
 
     // Output route.  Direct: on coherent hosts (Grace + NVLink-C2C, where the
     // device walks the host page tables) the kernel stores straight into the
@@ -974,37 +984,51 @@ namespace sbg
     }
     else
     {
-      uint64_t rb = 0;
-      while (rb < rows.n)
+      // Bands of whole row units, from the last row down.  Nothing overlaps
+      // the copy-out of the band computed last, and in a triangle the first
+      // rows hold the least output, so the schedule ends on them.  With
+      // automatic sizes the two lowest bands are cut into parts of about
+      // 1/2, 1/4, ... of their output, top part first, so the last copy is
+      // the first unit's output (about 2 MB for 1024 rows in float32), not
+      // a full band's.
+      const uint64_t units = (rows.n + align - 1) / align;
+      auto ustart = [&](uint64_t u) { return std::min<uint64_t>(rows.n, u * align); };
+      uint64_t ue = units;
+      while (ue > 0)
       {
-        uint64_t re = std::min<uint64_t>(rows.n, rb + align);
-        while (re < rows.n)
+        uint64_t ub = ue - 1;
+        while (ub > 0)
         {
-          uint64_t nxt = std::min<uint64_t>(rows.n, re + align);
-          uint64_t bytes = (row_output_start(mode, nxt, cs.n) - row_output_start(mode, rb, cs.n)) * sizeof(T);
+          const uint64_t bytes =
+              (row_output_start(mode, ustart(ue), cs.n) - row_output_start(mode, ustart(ub - 1), cs.n)) * sizeof(T);
           if (bytes > band_bytes) break;
-          re = nxt;
+          --ub;
         }
-        bands.emplace_back(rb, re);
-        rb = re;
+        bands.emplace_back(ustart(ub), ustart(ue));
+        ue = ub;
       }
-      // Nothing overlaps the last band's copy-out: with automatic sizes it
-      // is cut into parts of 1/2, 1/4, ... of its row units (one unit each
-      // at the end), so the exposed copy is about one unit's output.
       if (auto_bands && bands.size() > 1)
       {
-        const auto last = bands.back();
+        // The two lowest bands are cut again into parts of about half the
+        // remaining output each: every part's copy-out (about 3x faster than
+        // the kernel writes it) then hides behind the compute of the next,
+        // which is at least half its size, and the last part is unit 0.
         bands.pop_back();
-        uint64_t b0 = last.first;
-        uint64_t units = (last.second - b0 + align - 1) / align;
-        while (units > 1)
+        const auto above = bands.back();  // the lowest two end here
+        bands.pop_back();
+        uint64_t top = (above.second + align - 1) / align;
+        auto out_of = [&](uint64_t u0, uint64_t u1) {
+          return row_output_start(mode, ustart(u1), cs.n) - row_output_start(mode, ustart(u0), cs.n);
+        };
+        while (top > 1)
         {
-          const uint64_t take = units / 2;
-          bands.emplace_back(b0, b0 + take * align);
-          b0 += take * align;
-          units -= take;
+          const uint64_t half = out_of(0, top) / 2;
+          uint64_t ub = top - 1;
+          while (ub > 1 && out_of(ub, top) < half) --ub;
+          bands.emplace_back(ustart(ub), ustart(top));
+          top = ub;
         }
-        bands.emplace_back(b0, last.second);
+        bands.emplace_back(0, ustart(top));
       }
     }
     uint64_t max_band = 0;
@@ -1014,6 +1038,7 @@ namespace sbg
     DeviceBuffer obuf[2];
     for (int b = 0; b < nbuf; ++b) obuf[b].reset(std::max<uint64_t>(1, max_band) * sizeof(T));
     EventGuard computed[2], copied[2];
+    phases.mark("buffers");
 
     // Packed segment layout, once, for the global-memory variant.
     DeviceBuffer rpack, cpack;
@@ -1036,9 +1061,20 @@ namespace sbg
     }
     const int opk = op_kind(op, p);
 
+    // Bands alternate between two compute streams, one per output buffer:
+    // a band's CTAs start on the SMs that the previous band's last wave
+    // leaves idle, instead of after its last item.  Bands share nothing but
+    // the inputs, which the second stream waits for.
+    StreamGuard compute2;
+    EventGuard inputs_ready;
+    SBG_CUDA(cudaEventRecord(inputs_ready.e, compute.s));
+    SBG_CUDA(cudaStreamWaitEvent(compute2.s, inputs_ready.e, 0));
+    auto band_stream = [&](size_t k) { return (k % 2) ? compute2.s : compute.s; };
+
     auto launch_band = [&](size_t k) {
       const int b = (int)(k % 2);
-      if (k >= 2) SBG_CUDA(cudaStreamWaitEvent(compute.s, copied[b].e, 0));
+      const cudaStream_t bs = band_stream(k);
+      if (k >= 2) SBG_CUDA(cudaStreamWaitEvent(bs, copied[b].e, 0));
       ProblemDesc<T> d{};
       d.rpts = kr_pts; d.roff = drows.view.off; d.nr = rows.n;
       d.cpts = kc_pts; d.coff = (mode == MODE_CROSS) ? dcols.view.off : drows.view.off; d.nc = cs.n;
@@ -1052,8 +1088,14 @@ namespace sbg
       d.q = pl.q; d.mode = mode; d.p = (T)p;
       d.rcap = rows.off[rows.n];
       d.ccap = cs.off[cs.n];
-      launch_problem<T>(d, pl, opk, compute.s);
-      SBG_CUDA(cudaEventRecord(computed[b].e, compute.s));
+      // The small bands at the end of the schedule take fewer rows per item
+      // (the band starts stay multiples of the row chunk), so that each
+      // still gives the planner's 6 items per SM instead of ending on a
+      // ragged last wave.  No pair's arithmetic depends on the item shape.
+      if (!direct)
+        while (d.q > 1 && problem_item_count(d) < 6ull * (uint64_t)dev.sms) d.q /= 2;
+      launch_problem<T>(d, pl, opk, bs);
+      SBG_CUDA(cudaEventRecord(computed[b].e, bs));
     };
 
     bool cancelled = false;
@@ -1076,13 +1118,16 @@ namespace sbg
       SBG_CUDA(cudaStreamWaitEvent(copy.s, computed[b].e, 0));
       if (hi > lo) stager.copy(out + lo, obuf[b].as<T>(), (hi - lo) * sizeof(T), copy.s);
       stager.flush();
+      phases.mark("band", (long)k);
       SBG_CUDA(cudaEventRecord(copied[b].e, copy.s));
       if (ctl.progress) ctl.progress(hi - lo);
       if (ctl.stop && ctl.stop->load()) { cancelled = true; break; }
     }
     stager.flush();
     SBG_CUDA(cudaStreamSynchronize(compute.s));
+    SBG_CUDA(cudaStreamSynchronize(compute2.s));
     SBG_CUDA(cudaStreamSynchronize(copy.s));
+    phases.mark("synced");
     if (cancelled) throw Error(ST_CANCELLED, "task was cancelled");
   }
 
