@@ -444,8 +444,15 @@ namespace sbg
   // added to global memory once.  Lanes with no weight take no part and
   // leave zeros in their slots.  Column gradients leave as in the walks
   // above.
-  template <typename T, int OP, int W>
-  __global__ void __launch_bounds__(512) pairs_backward_window_kernel(const __grid_constant__ BwdParams<T> B)
+  //
+  // STAGED: the item's 32 columns are first copied into shared memory,
+  // element k of column l at [k * 32 + l] after the slots (B.cols_cap
+  // elements per column), so the walk reads them with conflict-free shared
+  // loads instead of one L1 request of 8 sectors per warp-step; the host
+  // picks it when the columns and the slots of 32 warps fit.
+  template <typename T, int OP, int W, bool STAGED>
+  __global__ void __launch_bounds__(STAGED ? 1024 : 512) pairs_backward_window_kernel(
+      const __grid_constant__ BwdParams<T> B)
   {
     static_assert(W >= 1 && W <= 16, "two lanes per window element");
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -453,9 +460,11 @@ namespace sbg
     __shared__ unsigned int s_next_row;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
     const unsigned FULL = 0xffffffffu;
     // slot (element j of the window, lane l) at [j * 32 + l]: (value-gradient term, time-gradient term)
     Elem<T>* slots = reinterpret_cast<Elem<T>*>(smem_raw) + (size_t)warp * W * 32;
+    Elem<T>* cols_s = reinterpret_cast<Elem<T>*>(smem_raw) + (size_t)nwarps * W * 32;
 
     for (;;)
     {
@@ -483,11 +492,25 @@ namespace sbg
       const uint64_t coff = B.off[corig];
       const uint32_t clen = (uint32_t)(B.off[corig + 1] - coff);
       const uint32_t maxlc = __reduce_max_sync(FULL, clen);  // warp-uniform: bounds the walk below
-      const bool item_ok = !__any_sync(FULL, clen == 0 || coff + clen > B.npts);
+      // Every warp of the CTA holds the same 32 columns, so item_ok (and
+      // with it the staging barrier below) is the same in all of them.  A
+      // column longer than the host's max_points (never expected) skips the
+      // item, as the other walks skip such rows.
+      const bool item_ok =
+          !__any_sync(FULL, clen == 0 || coff + clen > B.npts) && (!STAGED || maxlc <= B.cols_cap);
       if (item_ok)
       {
         const Elem<T>* col = B.pk + coff;
         T* cgrad = B.grad + 2 * coff;
+        if constexpr (STAGED)
+        {
+          for (uint32_t k = (uint32_t)warp; k < clen; k += (uint32_t)nwarps) cols_s[(size_t)k * 32 + lane] = col[k];
+          __syncthreads();
+        }
+        auto colat = [&](uint32_t k) -> Elem<T> {
+          if constexpr (STAGED) return cols_s[(size_t)k * 32 + lane];
+          else return col[k];
+        };
         for (;;)
         {
           unsigned r = 0;
@@ -518,7 +541,7 @@ namespace sbg
 
           const Elem<T>* row = B.pk + roff;
           Elem<T> F = row[0], F2 = row[rlen > 1 ? 1 : 0];
-          Elem<T> Gc = col[0], G2 = col[clen > 1 ? 1 : 0];
+          Elem<T> Gc = colat(0), G2 = colat(clen > 1 ? 1 : 0);
           uint32_t fi = 0, gi = 0;
           T t = T(0), accF = T(0), accG = T(0);
           for (uint32_t kb = 0; kb < rlen; kb += W)
@@ -561,7 +584,7 @@ namespace sbg
                   accG = T(0);
                   Gc = G2;
                   ++gi;
-                  G2 = col[min(gi + 1, clen - 1)];
+                  G2 = colat(min(gi + 1, clen - 1));
                 }
                 t = tn;
               }
@@ -742,14 +765,32 @@ namespace sbg
 #else
     const bool stage = false;
 #endif
-    B.cols_cap = stage ? lmax : 0;
+    // The windowed walk with the item's columns staged in shared memory:
+    // 32 warps and the widest window, 12 or 8 elements, whose slots fit
+    // beside the columns (float32 PCFs up to about 515 or 640 breakpoints).
+    // Forward + backward on GB300 (N = 4096 f32, L ~ U{16..512}; L2 kernel /
+    // L2 distance, ms): staged W = 12 16.5 / 17.3, W = 10 16.7 / 17.6,
+    // W = 8 17.0 / 17.9, W = 4 18.4 / 19.4; unstaged W = 16 18.4 / 19.3.
+#if defined(SBG_BWD_UNSTAGED)
+    constexpr bool ALLOW_STAGED = false;
+#else
+    constexpr bool ALLOW_STAGED = true;
+#endif
+    auto staged_fits = [&](int w) { return (size_t)32 * w * 32 * sizeof(Elem<T>) + cols_bytes <= budget; };
+    // float32 only: the f64 walk is bound by the FP64 pipe, and its staged
+    // form would spill at 32 warps.
+    const int BWD_WS =
+        (WINDOWED && ALLOW_STAGED && sizeof(T) == 4) ? (staged_fits(12) ? 12 : staged_fits(8) ? 8 : 0) : 0;
+    const bool wstage = BWD_WS > 0;
+    B.cols_cap = (stage || wstage) ? lmax : 0;
     const size_t fixed = stage ? cols_bytes : 0;
-    int warps = WINDOWED ? 16 : 32;
+    int warps = wstage ? 32 : WINDOWED ? 16 : 32;
     while (warps > 1 && fixed + (size_t)warps * grad_per_warp > budget) warps /= 2;
     if (stage) while (warps < 32 && fixed + (size_t)(warps + 8) * grad_per_warp <= budget) warps += 8;
-    // the windowed walk: one [BWD_W][32] slot array per warp
-    const size_t smem =
-        WINDOWED ? (size_t)warps * BWD_W * 32 * sizeof(Elem<T>) : fixed + (size_t)warps * grad_per_warp;
+    // the windowed walk: one [W][32] slot array per warp (then the staged columns)
+    const size_t smem = wstage     ? (size_t)warps * BWD_WS * 32 * sizeof(Elem<T>) + cols_bytes
+                        : WINDOWED ? (size_t)warps * BWD_W * 32 * sizeof(Elem<T>)
+                                   : fixed + (size_t)warps * grad_per_warp;
     if (smem > budget) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
     // The ordered-pairs variants measured slower on GB300 (N = 4096, L2
     // kernel): rows only, forward + backward 74 ms against 46 ms at the time
@@ -771,10 +812,19 @@ namespace sbg
     SBG_CUDA(cudaMemsetAsync(queue, 0, 8, st));
     if (B.total_items > 0)
     {
+      void (*staged_fn)(const BwdParams<T>) = nullptr;
+      if constexpr (sizeof(T) == 4)
+        staged_fn = BWD_WS == 12 ? (bop == BWD_INNER ? pairs_backward_window_kernel<T, BWD_INNER, 12, true>
+                                    : bop == BWD_L2DIST ? pairs_backward_window_kernel<T, BWD_L2DIST, 12, true>
+                                                        : pairs_backward_window_kernel<T, BWD_L1DIST, 12, true>)
+                                 : (bop == BWD_INNER ? pairs_backward_window_kernel<T, BWD_INNER, 8, true>
+                                    : bop == BWD_L2DIST ? pairs_backward_window_kernel<T, BWD_L2DIST, 8, true>
+                                                        : pairs_backward_window_kernel<T, BWD_L1DIST, 8, true>);
       void (*fn)(const BwdParams<T>) =
-          WINDOWED ? (bop == BWD_INNER ? pairs_backward_window_kernel<T, BWD_INNER, BWD_W>
-                      : bop == BWD_L2DIST ? pairs_backward_window_kernel<T, BWD_L2DIST, BWD_W>
-                                          : pairs_backward_window_kernel<T, BWD_L1DIST, BWD_W>)
+          wstage ? staged_fn
+          : WINDOWED ? (bop == BWD_INNER ? pairs_backward_window_kernel<T, BWD_INNER, BWD_W, false>
+                      : bop == BWD_L2DIST ? pairs_backward_window_kernel<T, BWD_L2DIST, BWD_W, false>
+                                          : pairs_backward_window_kernel<T, BWD_L1DIST, BWD_W, false>)
           : ROWSYNC ? (bop == BWD_INNER ? pairs_backward_rowsync_kernel<T, BWD_INNER>
                        : bop == BWD_L2DIST ? pairs_backward_rowsync_kernel<T, BWD_L2DIST>
                                            : pairs_backward_rowsync_kernel<T, BWD_L1DIST>)

@@ -116,3 +116,27 @@ def test_forward_of_autograd_path_equals_pdist():
     X = sb.PcfArray.from_csr(pts, off)
     np.testing.assert_allclose(ag.pdist(P, O, p=2).cpu().numpy(), sb.pdist(X, p=2).data, rtol=1e-5)
     np.testing.assert_allclose(ag.l2_kernel(P, O).cpu().numpy(), sb.l2_kernel(X).data, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("lengths", [(16, 500), (520, 620), (700, 900)])
+def test_backward_f32_walk_shapes(lengths):
+    """The float32 backward stages the item's columns in shared memory with
+    windows of 12 row elements while PCFs are short enough (up to about 515
+    breakpoints), with windows of 8 a little beyond, and reads them through
+    L1 with windows of 16 above that: each shape against the FP64 reference
+    gradient, L2 kernel and L1 distance."""
+    from stablebear_gb300 import synthetic
+    from tests.test_oracle import oracle_gradient
+    lo, hi = lengths
+    pts, off = synthetic.gaussian(70, synthetic.uniform_lengths(lo, hi), np.float32, seed=lo)
+    n = len(off) - 1
+    mask = np.ones(pts.shape, bool)
+    mask[(off[1:] - 1).astype(int), 1] = False
+    mask[off[:-1].astype(int), 0] = False
+    for kind, op, mode in (("l2_kernel", 2, 2), ("l1", 0, 1)):
+        cnt = n * (n + 1) // 2 if mode == 2 else n * (n - 1) // 2
+        w = np.random.default_rng(lo + mode).standard_normal(cnt).astype(np.float32)
+        g, M = _grad_gpu(pts, off, kind, w)
+        ref = oracle_gradient(pts.astype(np.float64), off, op, mode, w.astype(np.float64), None)
+        err = np.abs(g - ref)[mask].max() / np.abs(ref[mask]).max()
+        assert err <= 2e-4, (kind, lengths, err)
