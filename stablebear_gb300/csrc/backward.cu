@@ -539,14 +539,23 @@ namespace sbg
           if (!live)
             for (int j = 0; j < W; ++j) slots[j * 32 + lane] = Elem<T>{T(0), T(0)};
 
+          // Next elements are read one (column) or two (row) places past a
+          // PCF's end without a clamp: the packed layout has two spare
+          // elements after the last PCF and the staged columns one spare
+          // row, and a value read there is never used (a side's last element
+          // ends at TMAX, so it is never left before the walk ends).
           const Elem<T>* row = B.pk + roff;
-          Elem<T> F = row[0], F2 = row[rlen > 1 ? 1 : 0];
-          Elem<T> Gc = colat(0), G2 = colat(clen > 1 ? 1 : 0);
+          Elem<T> F = row[0], F2 = row[1];
+          const Elem<T>* rnext = row + 2;
+          Elem<T> Gc = colat(0), G2 = colat(1);
           uint32_t fi = 0, gi = 0;
+          T* cgp = cgrad;
           T t = T(0), accF = T(0), accG = T(0);
           for (uint32_t kb = 0; kb < rlen; kb += W)
           {
             const uint32_t ke = min(kb + (uint32_t)W, rlen);
+            const uint32_t kel = live ? ke : 0u;  // lanes with no weight take no step
+            Elem<T>* sp = slots + lane;           // this lane's slot for row element fi (fi == kb here)
             // Walk until this lane has left row element ke - 1 (for the last
             // element: taken the last rectangle, to TMAX).  A lane takes at
             // most W row steps and clen - 1 column steps in a window, so the
@@ -554,7 +563,7 @@ namespace sbg
             // in every lane, so all 32 lanes run every iteration's vote.
             for (uint32_t guard = 0; guard <= (uint32_t)W + maxlc; ++guard)
             {
-              const bool act = live && fi < ke;
+              const bool act = fi < kel;
               if (!__any_sync(FULL, act)) break;
               if (act)
               {
@@ -570,21 +579,23 @@ namespace sbg
                   // leave row element fi; a breakpoint shared with the
                   // column, or the row's end, has no time gradient
                   const T dF = (F.tn == Gc.tn || fi + 1 >= rlen) ? T(0) : w * step_delta<OP>(F.v, F2.v, Gc.v);
-                  slots[(fi - kb) * 32 + lane] = Elem<T>{w * accF, dF};
+                  *sp = Elem<T>{w * accF, dF};
+                  sp += 32;
                   accF = T(0);
                   F = F2;
                   ++fi;
-                  F2 = row[min(fi + 1, rlen - 1)];
+                  F2 = *rnext++;
                 }
                 else
                 {
                   // Gc.tn < F.tn <= TMAX: the column has a next element, G2
                   const T dG = (dt == T(0)) ? T(0) : w * step_delta<OP>(Gc.v, G2.v, F.v);
-                  red_add2(&cgrad[2 * (size_t)gi], w * accG, dG);
+                  red_add2(cgp, w * accG, dG);
+                  cgp += 2;
                   accG = T(0);
                   Gc = G2;
                   ++gi;
-                  G2 = colat(min(gi + 1, clen - 1));
+                  G2 = colat(gi + 1);
                 }
                 t = tn;
               }
@@ -611,7 +622,7 @@ namespace sbg
             if (h == 0 && j < nel && (sv != T(0) || st != T(0))) red_add2(&B.grad[2 * (roff + kb + j)], sv, st);
             __syncwarp();
           }
-          if (live) atomicAdd(&cgrad[2 * (size_t)gi], w * accG);
+          if (live) atomicAdd(cgp, w * accG);
         }
       }
       __syncthreads();
@@ -693,7 +704,9 @@ namespace sbg
     SBG_CUDA(cudaMemsetAsync(grad, 0, sizeof(T) * 2 * npts, st));
     if (n == 0) return;
 
-    StreamBuffer packed_buf(std::max<uint64_t>(1, npts) * sizeof(Elem<T>), st);
+    // two spare elements after the last PCF: the windowed walk reads up to
+    // two places past a PCF's end (values it never uses)
+    StreamBuffer packed_buf((npts + 2) * sizeof(Elem<T>), st);
     StreamBuffer queue_buf(256, st);
     StreamBuffer paired_buf(std::max<uint64_t>(1, npts) * 2 * sizeof(T), st);
     StreamBuffer order_buf(n * sizeof(uint32_t), st);
@@ -776,7 +789,9 @@ namespace sbg
 #else
     constexpr bool ALLOW_STAGED = true;
 #endif
-    auto staged_fits = [&](int w) { return (size_t)32 * w * 32 * sizeof(Elem<T>) + cols_bytes <= budget; };
+    // the staged columns keep one spare row (the walk reads one place past a column's end)
+    const size_t scols_bytes = (size_t)32 * (lmax + 1) * sizeof(Elem<T>);
+    auto staged_fits = [&](int w) { return (size_t)32 * w * 32 * sizeof(Elem<T>) + scols_bytes <= budget; };
     // float32 only: the f64 walk is bound by the FP64 pipe, and its staged
     // form would spill at 32 warps.
     const int BWD_WS =
@@ -788,7 +803,7 @@ namespace sbg
     while (warps > 1 && fixed + (size_t)warps * grad_per_warp > budget) warps /= 2;
     if (stage) while (warps < 32 && fixed + (size_t)(warps + 8) * grad_per_warp <= budget) warps += 8;
     // the windowed walk: one [W][32] slot array per warp (then the staged columns)
-    const size_t smem = wstage     ? (size_t)warps * BWD_WS * 32 * sizeof(Elem<T>) + cols_bytes
+    const size_t smem = wstage     ? (size_t)warps * BWD_WS * 32 * sizeof(Elem<T>) + scols_bytes
                         : WINDOWED ? (size_t)warps * BWD_W * 32 * sizeof(Elem<T>)
                                    : fixed + (size_t)warps * grad_per_warp;
     if (smem > budget) throw Error(ST_INVALID_ARGUMENT, "PCFs too long for the backward kernel's row buffers");
