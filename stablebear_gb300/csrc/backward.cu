@@ -759,11 +759,12 @@ namespace sbg
 #endif
     constexpr bool ROWSYNC = WALK == 1 && SIDE == 0 && !WI && !defined_stage_columns();
     constexpr bool WINDOWED = WALK == 2 && SIDE == 0 && !WI && !defined_stage_columns();
-    // Forward + backward on GB300 (N = 4096 f32, L ~ U{16..512}; L2 kernel /
-    // L2 distance, ms): W = 4 21.6 / 22.4, W = 8 19.5 / 20.2, W = 16
-    // 18.6 / 19.2; the row-synchronous walk 18.5 / 19.6; the free-running
-    // walk with per-warp buffers 24.7 / 24.8.  W = 16 holds 64 KB of slots
-    // per 16-warp block in f32 and 128 KB in f64.
+    // The windowed walk with columns read through L1 (f64, long PCFs, or
+    // SBG_BWD_UNSTAGED).  Forward + backward on GB300 (N = 4096 f32,
+    // L ~ U{16..512}; L2 kernel / L2 distance, ms): W = 4 21.6 / 22.4,
+    // W = 8 19.5 / 20.2, W = 16 18.4 / 19.3; the row-synchronous walk
+    // 18.5 / 19.6; the free-running walk with per-warp buffers 24.7 / 24.8.
+    // W = 16 holds 64 KB of slots per 16-warp block in f32 and 128 KB in f64.
 #ifndef SBG_BWD_WINDOW
 #define SBG_BWD_WINDOW 16
 #endif
