@@ -556,49 +556,52 @@ namespace sbg
             const uint32_t ke = min(kb + (uint32_t)W, rlen);
             const uint32_t kel = live ? ke : 0u;  // lanes with no weight take no step
             Elem<T>* sp = slots + lane;           // this lane's slot for row element fi (fi == kb here)
+            // One step of the walk (the lane's next rectangle).
+            auto step = [&]() {
+              const bool takeF = row_first(F.tn, Gc.tn);
+              const T tn = takeF ? F.tn : Gc.tn;
+              const T dt = tn - t;
+              T cf, cg;
+              seg_coeffs<OP>(F.v, Gc.v, cf, cg);
+              accF = fma(dt, cf, accF);
+              accG = fma(dt, cg, accG);
+              if (takeF)
+              {
+                // leave row element fi; a breakpoint shared with the
+                // column, or the row's end, has no time gradient
+                const T dF = (F.tn == Gc.tn || fi + 1 >= rlen) ? T(0) : w * step_delta<OP>(F.v, F2.v, Gc.v);
+                *sp = Elem<T>{w * accF, dF};
+                sp += 32;
+                accF = T(0);
+                F = F2;
+                ++fi;
+                F2 = *rnext++;
+              }
+              else
+              {
+                // Gc.tn < F.tn <= TMAX: the column has a next element, G2
+                const T dG = (dt == T(0)) ? T(0) : w * step_delta<OP>(Gc.v, G2.v, F.v);
+                red_add2(cgp, w * accG, dG);
+                cgp += 2;
+                accG = T(0);
+                Gc = G2;
+                ++gi;
+                G2 = colat(gi + 1);
+              }
+              t = tn;
+            };
             // Walk until this lane has left row element ke - 1 (for the last
             // element: taken the last rectangle, to TMAX).  A lane takes at
             // most W row steps and clen - 1 column steps in a window, so the
             // bound W + maxlc ends the loop whatever the data; it is the same
             // in every lane, so all 32 lanes run every iteration's vote.
+            // Two steps per vote; a lane that leaves the window after the
+            // first takes no second one.
             for (uint32_t guard = 0; guard <= (uint32_t)W + maxlc; ++guard)
             {
-              const bool act = fi < kel;
-              if (!__any_sync(FULL, act)) break;
-              if (act)
-              {
-                const bool takeF = row_first(F.tn, Gc.tn);
-                const T tn = takeF ? F.tn : Gc.tn;
-                const T dt = tn - t;
-                T cf, cg;
-                seg_coeffs<OP>(F.v, Gc.v, cf, cg);
-                accF = fma(dt, cf, accF);
-                accG = fma(dt, cg, accG);
-                if (takeF)
-                {
-                  // leave row element fi; a breakpoint shared with the
-                  // column, or the row's end, has no time gradient
-                  const T dF = (F.tn == Gc.tn || fi + 1 >= rlen) ? T(0) : w * step_delta<OP>(F.v, F2.v, Gc.v);
-                  *sp = Elem<T>{w * accF, dF};
-                  sp += 32;
-                  accF = T(0);
-                  F = F2;
-                  ++fi;
-                  F2 = *rnext++;
-                }
-                else
-                {
-                  // Gc.tn < F.tn <= TMAX: the column has a next element, G2
-                  const T dG = (dt == T(0)) ? T(0) : w * step_delta<OP>(Gc.v, G2.v, F.v);
-                  red_add2(cgp, w * accG, dG);
-                  cgp += 2;
-                  accG = T(0);
-                  Gc = G2;
-                  ++gi;
-                  G2 = colat(gi + 1);
-                }
-                t = tn;
-              }
+              if (!__any_sync(FULL, fi < kel)) break;
+              if (fi < kel) step();
+              if (fi < kel) step();
             }
             __syncwarp();
             // element j of the window: lanes j and j + 16 each sum 16 of its
