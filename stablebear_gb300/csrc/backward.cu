@@ -788,6 +788,8 @@ namespace sbg
     // Forward + backward on GB300 (N = 4096 f32, L ~ U{16..512}; L2 kernel /
     // L2 distance, ms): staged W = 12 16.5 / 17.3, W = 10 16.7 / 17.6,
     // W = 8 17.0 / 17.9, W = 4 18.4 / 19.4; unstaged W = 16 18.4 / 19.3.
+    // Staged W = 16 fits 24 warps only: 16.3 / 16.3 against 16.2 / 16.2 for
+    // W = 12 with 32 warps (both with two steps per vote).
 #if defined(SBG_BWD_UNSTAGED)
     constexpr bool ALLOW_STAGED = false;
 #else
