@@ -412,6 +412,14 @@ int sbg_condensed_to_dense_device(int dtype, int skip_mode, uint64_t n, const vo
 int sbg_dense_to_condensed_device(int dtype, int skip_mode, uint64_t n, const void* dense, uint64_t ld,
                                   void* condensed, unsigned int* flags, void* stream);
 
+/* The adjoint of the symmetric expansion (sbg_condensed_to_dense_device):
+ * each stored entry receives dense[i][j] + dense[j][i], i > j, and for
+ * SymmetricMatrix storage the diagonal entry dense[i][i]; nothing is
+ * checked.  This maps dL/d(dense) to dL/d(condensed) for gradients through
+ * the expansion.  No counterpart in the reference (it has no gradients). */
+int sbg_dense_fold_to_condensed_device(int dtype, int skip_mode, uint64_t n, const void* dense, uint64_t ld,
+                                       void* condensed, void* stream);
+
 /* ---- single-PCF integrals --------------------------------------------------- */
 
 /* out[i] = ||f_i||_p over [0, inf) for the n PCFs of the CSR (p >= 1): the

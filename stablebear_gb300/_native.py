@@ -100,6 +100,7 @@ SIGNATURES = {
     "sbg_enumerate_items": (_U64, [_I, _U64, _U64, _U64, _U64, ctypes.c_uint32, _P, _U64]),
     "sbg_condensed_to_dense_device": (_I, [_I, _I, _U64, _P, _P, _U64, _U64, _U64, _P]),
     "sbg_dense_to_condensed_device": (_I, [_I, _I, _U64, _P, _U64, _P, _P, _P]),
+    "sbg_dense_fold_to_condensed_device": (_I, [_I, _I, _U64, _P, _U64, _P, _P]),
     "sbg_lp_norm_device": (_I, [_I, _D, _P, _P, _U64, _P, _P]),
     "sbg_lp_norm_host": (_I, [_I, _D, _P, _P, _U64, _P]),
     "sbg_iterate_rectangles": (_I, [_I, _P, _U64, _P, _U64, _D, _D, _P, _U64, _P]),

@@ -85,10 +85,39 @@ def pdist(points, offsets, p=2):
     return PairwiseIntegral.apply(points, offsets, "l1" if p == 1 else "l2", _max_points(offsets))
 
 
+class _SymmetricExpand(torch.autograd.Function):
+    """Condensed storage to the symmetric dense matrix on the device
+    (``sbg_condensed_to_dense_device``); its gradient folds both mirror
+    entries of dL/d(dense) back into the stored one
+    (``sbg_dense_fold_to_condensed_device``)."""
+
+    @staticmethod
+    def forward(ctx, c, n, diagonal):
+        skip = nat.SKIP_LOWER if diagonal else nat.SKIP_LOWER_NODIAG
+        n = int(n)
+        c = c.contiguous()
+        if c.numel() != int(nat.lib().sbg_output_count(skip, n, n)):
+            raise ValueError(f"a condensed vector of {c.numel()} values is not a {n} x {n} matrix of this kind")
+        dense = torch.empty((n, n), dtype=c.dtype, device=c.device)
+        if n:
+            nat.check(nat.lib().sbg_condensed_to_dense_device(_code(c), skip, n, c.data_ptr(), dense.data_ptr(), n, 0,
+                                                              n, _stream(c.device)))
+        ctx.n, ctx.skip = n, skip
+        return dense
+
+    @staticmethod
+    def backward(ctx, grad_dense):
+        g = grad_dense.contiguous()
+        n = ctx.n
+        gc = torch.empty(int(nat.lib().sbg_output_count(ctx.skip, n, n)), dtype=g.dtype, device=g.device)
+        if n and gc.numel():
+            nat.check(nat.lib().sbg_dense_fold_to_condensed_device(_code(g), ctx.skip, n, g.data_ptr(), n,
+                                                                   gc.data_ptr(), _stream(g.device)))
+        return gc, None, None
+
+
 def condensed_to_dense(c, n, diagonal):
-    """Expand a condensed vector to the symmetric n x n matrix (differentiable)."""
-    k = 0 if diagonal else -1
-    r, s = torch.tril_indices(n, n, offset=k, device=c.device)
-    dense = torch.zeros(n, n, dtype=c.dtype, device=c.device)
-    dense = dense.index_put((r, s), c)
-    return dense + torch.tril(dense, -1).transpose(0, 1)
+    """Expand a condensed vector to the symmetric n x n matrix (differentiable):
+    ``diagonal`` True for SymmetricMatrix order (the L2 kernel), False for
+    DistanceMatrix order (zero diagonal)."""
+    return _SymmetricExpand.apply(c, n, diagonal)

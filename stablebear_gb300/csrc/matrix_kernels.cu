@@ -177,10 +177,13 @@ namespace sbg
 
     // Flags (bit set = violated somewhere): 1 not symmetric, 2 non-zero
     // diagonal (distance matrices), 4 negative entry (distance matrices).
+    // FOLD: no checks; each stored entry receives dense[i][j] + dense[j][i]
+    // (the diagonal itself for symmetric-matrix storage), the adjoint of the
+    // symmetric expansion, which gradients through it need.
     // TD x TD tiles (TD = 64: each row piece of a tile, and of its mirror,
     // is 256 contiguous bytes read by two warps, against 128 with 32-wide
     // tiles; the reads of the two triangles dominate this kernel's traffic).
-    template <typename T, int TD>
+    template <typename T, int TD, bool FOLD = false>
     __global__ void __launch_bounds__(TD * ROWS) dense_to_condensed_kernel(
         const T* __restrict__ dense, uint64_t n, uint64_t ld, bool diag, T* __restrict__ cond,
         unsigned int* __restrict__ flags, TileSet ts)
@@ -215,9 +218,14 @@ namespace sbg
           for (int q = 0; q < TD / ROWS; ++q)
           {
             const T v = low[q];
-            if (!(v == upper[ty + q * ROWS][tx])) f |= 1u;
-            if (!diag && v < T(0)) f |= 4u;
-            dst[0] = v;
+            if constexpr (FOLD)
+              dst[0] = v + upper[ty + q * ROWS][tx];
+            else
+            {
+              if (!(v == upper[ty + q * ROWS][tx])) f |= 1u;
+              if (!diag && v < T(0)) f |= 4u;
+              dst[0] = v;
+            }
             dst += ROWS * i + (diag ? ROWS * (ROWS + 1) / 2 : ROWS * (ROWS - 1) / 2);
             i += ROWS;
           }
@@ -242,7 +250,18 @@ namespace sbg
         {
           const int r = ty + q * ROWS;
           const uint64_t i = i0 + r, j = j0 + tx;
-          if (i < n && j < n && j <= i)
+          if (FOLD && i < n && j < n && j <= i)
+          {
+            // the adjoint of the symmetric expansion: both mirror entries
+            // flow into the one stored value, the diagonal into itself
+            if (j == i)
+            {
+              if (diag) cond[cond_index(true, i, j)] = low[q];
+            }
+            else
+              cond[cond_index(diag, i, j)] = low[q] + upper[r][tx];
+          }
+          else if (!FOLD && i < n && j < n && j <= i)
           {
             const T v = low[q];
             if (!(v == upper[r][tx])) f |= 1u;  // NaN counts as asymmetric, as != does in the reference
@@ -260,8 +279,11 @@ namespace sbg
         }
         __syncthreads();
       }
-      f = __reduce_or_sync(0xffffffffu, f);
-      if (f && (threadIdx.x & 31) == 0) atomicOr(flags, f);
+      if constexpr (!FOLD)
+      {
+        f = __reduce_or_sync(0xffffffffu, f);
+        if (f && (threadIdx.x & 31) == 0) atomicOr(flags, f);
+      }
     }
 
     template <typename F>
@@ -355,6 +377,34 @@ extern "C"
       else
         dense_to_condensed_kernel<double, TD><<<grid, block, 0, st>>>((const double*)dense, n, ld, diag,
                                                                        (double*)condensed, flags, ts);
+      SBG_CUDA(launched());
+    });
+  }
+
+  int sbg_dense_fold_to_condensed_device(int dtype, int skip, uint64_t n, const void* dense, uint64_t ld,
+                                         void* condensed, void* stream)
+  {
+    return abi_call([&] {
+      check_kind(dtype, skip);
+      if (n == 0) return;
+      if (ld < n) throw Error(ST_INVALID_ARGUMENT, "ld must be >= n");
+      if (!dense || (!condensed && output_count(skip, n, n) > 0))
+        throw Error(ST_INVALID_ARGUMENT, "null matrix pointer");
+      constexpr int TD = D2C_TILE;
+      const uint64_t nb = ceil_div_u64(n, TD);
+      TileSet ts;
+      ts.init(0, nb, nb);
+      cudaStream_t st = (cudaStream_t)stream;
+      const dim3 block(TD, ROWS);
+      const int grid = (int)std::min<uint64_t>(std::max<uint64_t>(ts.count, 1),
+                                               (uint64_t)device_info().sms * (2048 / (TD * ROWS)));
+      const bool diag = skip == SBG_SKIP_LOWER;
+      if (dtype == SBG_F32)
+        dense_to_condensed_kernel<float, TD, true><<<grid, block, 0, st>>>((const float*)dense, n, ld, diag,
+                                                                            (float*)condensed, nullptr, ts);
+      else
+        dense_to_condensed_kernel<double, TD, true><<<grid, block, 0, st>>>((const double*)dense, n, ld, diag,
+                                                                             (double*)condensed, nullptr, ts);
       SBG_CUDA(launched());
     });
   }

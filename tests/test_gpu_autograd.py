@@ -140,3 +140,36 @@ def test_backward_f32_walk_shapes(lengths):
         ref = oracle_gradient(pts.astype(np.float64), off, op, mode, w.astype(np.float64), None)
         err = np.abs(g - ref)[mask].max() / np.abs(ref[mask]).max()
         assert err <= 2e-4, (kind, lengths, err)
+
+
+def _torch_expand(c, n, diagonal):
+    import torch
+    k = 0 if diagonal else -1
+    r, s = torch.tril_indices(n, n, offset=k, device=c.device)
+    dense = torch.zeros(n, n, dtype=c.dtype, device=c.device)
+    dense = dense.index_put((r, s), c)
+    return dense + torch.tril(dense, -1).transpose(0, 1)
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+@pytest.mark.parametrize("diagonal", [True, False])
+@pytest.mark.parametrize("n", [1, 2, 65, 300])
+def test_condensed_to_dense_and_its_gradient(dtype, diagonal, n):
+    """The native expansion (sbg_condensed_to_dense_device) and its gradient
+    (sbg_dense_fold_to_condensed_device) against the same expansion written
+    with torch indexing ops: both bit for bit (the gradient of an
+    off-diagonal entry is G_ij + G_ji either way)."""
+    import torch
+    from stablebear_gb300 import autograd as ag
+    dt = getattr(torch, dtype)
+    cnt = n * (n + 1) // 2 if diagonal else n * (n - 1) // 2
+    gen = torch.Generator("cuda").manual_seed(n + (7 if diagonal else 0))
+    c = torch.randn(cnt, dtype=dt, device="cuda", generator=gen).requires_grad_(True)
+    G = torch.randn(n, n, dtype=dt, device="cuda", generator=gen)
+    c2 = c.detach().clone().requires_grad_(True)
+    D = ag.condensed_to_dense(c, n, diagonal)
+    (G * D).sum().backward()
+    D2 = _torch_expand(c2, n, diagonal)
+    (G * D2).sum().backward()
+    assert torch.equal(D, D2)
+    assert torch.equal(c.grad, c2.grad)
