@@ -238,13 +238,15 @@ def run_aux(args):
         O = torch.tensor(off.astype(np.int64), device="cuda")
         G = torch.randn(n, n, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
         G = G + G.T
+        lmax = int(np.diff(off.astype(np.int64)).max())
         segs_kernel = synthetic.segment_count(off, pts, 2)
         segs_dist = synthetic.segment_count(off, pts, 1)
         for name in ("l2_kernel", "l2"):
             diag = name == "l2_kernel"
 
             def fwd():
-                return ag.l2_kernel(P, O) if diag else ag.pdist(P, O, p=2)
+                # the longest PCF's length is known on the host, as for the device entry
+                return ag.l2_kernel(P, O, max_points=lmax) if diag else ag.pdist(P, O, p=2, max_points=lmax)
 
             def fwdbwd():
                 P.grad = None

@@ -73,16 +73,22 @@ def _max_points(offsets):
     return int((offsets[1:] - offsets[:-1]).max().item()) if offsets.numel() > 1 else 1
 
 
-def l2_kernel(points, offsets):
-    """Condensed L2 Gram matrix (SymmetricMatrix order), differentiable."""
-    return PairwiseIntegral.apply(points, offsets, "l2_kernel", _max_points(offsets))
+def l2_kernel(points, offsets, max_points=None):
+    """Condensed L2 Gram matrix (SymmetricMatrix order), differentiable.
+    ``max_points``: the largest PCF's breakpoint count, if the caller knows
+    it (otherwise it is read from ``offsets``, which synchronises the
+    stream); it must not be smaller than the true one."""
+    mp = _max_points(offsets) if max_points is None else int(max_points)
+    return PairwiseIntegral.apply(points, offsets, "l2_kernel", mp)
 
 
-def pdist(points, offsets, p=2):
-    """Condensed L1 or L2 distance matrix (DistanceMatrix order), differentiable."""
+def pdist(points, offsets, p=2, max_points=None):
+    """Condensed L1 or L2 distance matrix (DistanceMatrix order), differentiable;
+    ``max_points`` as for ``l2_kernel``."""
     if p not in (1, 2):
         raise ValueError("gradients are implemented for p = 1 and p = 2")
-    return PairwiseIntegral.apply(points, offsets, "l1" if p == 1 else "l2", _max_points(offsets))
+    mp = _max_points(offsets) if max_points is None else int(max_points)
+    return PairwiseIntegral.apply(points, offsets, "l1" if p == 1 else "l2", mp)
 
 
 class _SymmetricExpand(torch.autograd.Function):

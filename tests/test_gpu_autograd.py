@@ -173,3 +173,23 @@ def test_condensed_to_dense_and_its_gradient(dtype, diagonal, n):
     (G * D2).sum().backward()
     assert torch.equal(D, D2)
     assert torch.equal(c.grad, c2.grad)
+
+
+def test_given_max_points_changes_nothing():
+    """A caller that knows the longest PCF passes max_points and skips the
+    read-back: the same forward result bit for bit, and the same gradient up
+    to the order of its atomic float32 additions."""
+    import torch
+    from stablebear_gb300 import autograd as ag, synthetic
+    pts, off = synthetic.differentiation(160, seed=5)
+    lmax = int(np.diff(off.astype(np.int64)).max())
+    O = torch.tensor(off.astype(np.int64), device="cuda")
+    out = []
+    for mp in (None, lmax):
+        P = torch.tensor(pts, device="cuda", requires_grad=True)
+        M = ag.l2_kernel(P, O, max_points=mp)
+        (M * M).sum().backward()
+        out.append((M.detach().clone(), P.grad.clone()))
+    assert torch.equal(out[0][0], out[1][0])
+    g0, g1 = out[0][1], out[1][1]
+    assert float((g0 - g1).abs().max()) <= 1e-5 * float(g0.abs().max())
