@@ -824,7 +824,14 @@ namespace sbg
     // were not colliding; they stay available behind SBG_BWD_WARP_ITEMS.
     const uint64_t G = ceil_div_u64(n, 32);
     auto items = [&](uint32_t qq) { return SQ ? ceil_div_u64(n, 32ull * qq) * G : tri_item_count(0, n, qq, G); };
-    const uint64_t want_items = (uint64_t)dev.sms * (WI ? warps * 4 : 6);
+    // At least 12 work items per SM, with the largest rows per item (up to
+    // 256) that give them: forward + backward at N = 4096 (L2 kernel)
+    // measured 15.10 ms with 6 items per SM, 14.84 with 12, 14.81 with 24
+    // and 14.92 with 48.
+#ifndef SBG_BWD_ITEMS_PER_SM
+#define SBG_BWD_ITEMS_PER_SM 12
+#endif
+    const uint64_t want_items = (uint64_t)dev.sms * (WI ? warps * 4 : SBG_BWD_ITEMS_PER_SM);
     uint32_t q = 1;
     for (uint32_t cand = 8; cand >= 1; cand /= 2)
       if (items(cand) >= want_items) { q = cand; break; }
