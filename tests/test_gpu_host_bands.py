@@ -59,3 +59,26 @@ def test_auto_bands_match_device_entry(capfd):
     assert len(line) == 1
     bands = [tok for tok in line[0].split() if tok.startswith("band")]
     assert len(bands) > 8 and "synced" in line[0] and "freed" in line[0]
+
+
+def test_auto_bands_cdist_match_device_entry():
+    """The same schedule on a dense cross (cdist) output, whose rows all hold
+    the same output: 12,000 x 12,000 float32 (576 MB)."""
+    import torch
+    import stablebear_gb300 as sb
+    from stablebear_gb300 import _native as nat, synthetic
+    nr = nc = 12000
+    xp, xo = synthetic.gaussian(nr, synthetic.uniform_lengths(4, 20), np.float32, seed=31)
+    yp, yo = synthetic.gaussian(nc, synthetic.uniform_lengths(4, 20), np.float32, seed=32)
+    assert nr * nc * 4 > 512 << 20
+    got = sb.cdist(sb.PcfArray.from_csr(xp, xo), sb.PcfArray.from_csr(yp, yo), p=1)
+    lmax = int(max(np.diff(xo.astype(np.int64)).max(), np.diff(yo.astype(np.int64)).max()))
+    dx, dxo = torch.from_numpy(xp).cuda(), torch.from_numpy(xo.astype(np.int64)).cuda()
+    dy, dyo = torch.from_numpy(yp).cuda(), torch.from_numpy(yo.astype(np.int64)).cuda()
+    out = torch.full((nr * nc,), float("nan"), dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    nat.check(nat.lib().sbg_pairwise_device(nat.F32, nat.OP_L1, 1.0, nat.SKIP_NONE, dx.data_ptr(), dxo.data_ptr(),
+                                            nr, dy.data_ptr(), dyo.data_ptr(), nc, None, None, lmax,
+                                            out.data_ptr(), 0, 0, 0, ctypes.c_void_p(st)))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(np.asarray(got).reshape(-1), out.cpu().numpy())
