@@ -551,42 +551,61 @@ namespace sbg
           uint32_t fi = 0, gi = 0;
           T* cgp = cgrad;
           T t = T(0), accF = T(0), accG = T(0);
+          T wF = w * F.v, wG = w * Gc.v;  // used by the L2 kernel's walk only
           for (uint32_t kb = 0; kb < rlen; kb += W)
           {
             const uint32_t ke = min(kb + (uint32_t)W, rlen);
             const uint32_t kel = live ? ke : 0u;  // lanes with no weight take no step
             Elem<T>* sp = slots + lane;           // this lane's slot for row element fi (fi == kb here)
-            // One step of the walk (the lane's next rectangle).
+            // One step of the walk (the lane's next rectangle).  For the L2
+            // kernel the weight rides on each side's value (wF = w F.v,
+            // wG = w Gc.v, renewed when a side moves), so a flush multiplies
+            // by nothing more.
             auto step = [&]() {
               const bool takeF = row_first(F.tn, Gc.tn);
               const T tn = takeF ? F.tn : Gc.tn;
               const T dt = tn - t;
-              T cf, cg;
-              seg_coeffs<OP>(F.v, Gc.v, cf, cg);
-              accF = fma(dt, cf, accF);
-              accG = fma(dt, cg, accG);
+              if constexpr (OP == BWD_INNER)
+              {
+                accF = fma(dt, wG, accF);
+                accG = fma(dt, wF, accG);
+              }
+              else
+              {
+                T cf, cg;
+                seg_coeffs<OP>(F.v, Gc.v, cf, cg);
+                accF = fma(dt, cf, accF);
+                accG = fma(dt, cg, accG);
+              }
               if (takeF)
               {
                 // leave row element fi; a breakpoint shared with the
                 // column, or the row's end, has no time gradient
-                const T dF = (F.tn == Gc.tn || fi + 1 >= rlen) ? T(0) : w * step_delta<OP>(F.v, F2.v, Gc.v);
-                *sp = Elem<T>{w * accF, dF};
+                const bool none = F.tn == Gc.tn || fi + 1 >= rlen;
+                if constexpr (OP == BWD_INNER)
+                  *sp = Elem<T>{accF, none ? T(0) : (F.v - F2.v) * wG};
+                else
+                  *sp = Elem<T>{w * accF, none ? T(0) : w * step_delta<OP>(F.v, F2.v, Gc.v)};
                 sp += 32;
                 accF = T(0);
                 F = F2;
                 ++fi;
                 F2 = *rnext++;
+                if constexpr (OP == BWD_INNER) wF = w * F.v;
               }
               else
               {
                 // Gc.tn < F.tn <= TMAX: the column has a next element, G2
-                const T dG = (dt == T(0)) ? T(0) : w * step_delta<OP>(Gc.v, G2.v, F.v);
-                red_add2(cgp, w * accG, dG);
+                if constexpr (OP == BWD_INNER)
+                  red_add2(cgp, accG, dt == T(0) ? T(0) : (Gc.v - G2.v) * wF);
+                else
+                  red_add2(cgp, w * accG, dt == T(0) ? T(0) : w * step_delta<OP>(Gc.v, G2.v, F.v));
                 cgp += 2;
                 accG = T(0);
                 Gc = G2;
                 ++gi;
                 G2 = colat(gi + 1);
+                if constexpr (OP == BWD_INNER) wG = w * Gc.v;
               }
               t = tn;
             };
@@ -625,7 +644,7 @@ namespace sbg
             if (h == 0 && j < nel && (sv != T(0) || st != T(0))) red_add2(&B.grad[2 * (roff + kb + j)], sv, st);
             __syncwarp();
           }
-          if (live) atomicAdd(cgp, w * accG);
+          if (live) atomicAdd(cgp, OP == BWD_INNER ? accG : w * accG);
         }
       }
       __syncthreads();
