@@ -560,7 +560,9 @@ namespace sbg
             // One step of the walk (the lane's next rectangle).  For the L2
             // kernel the weight rides on each side's value (wF = w F.v,
             // wG = w Gc.v, renewed when a side moves), so a flush multiplies
-            // by nothing more.
+            // by nothing more.  (The same for the L2 distance, whose step
+            // term then reads (a - b)(wa + wb - 2 wo) / 2, measured slower:
+            // 15.29 against 14.89 ms forward + backward at N = 4096.)
             auto step = [&]() {
               const bool takeF = row_first(F.tn, Gc.tn);
               const T tn = takeF ? F.tn : Gc.tn;
