@@ -33,6 +33,12 @@ def _code(t):
     raise TypeError("points must be float32 or float64")
 
 
+def _need_cuda(*tensors):
+    for t in tensors:
+        if not t.is_cuda:
+            raise ValueError("the differentiable functions take CUDA tensors (the kernels read device memory)")
+
+
 def _stream(dev):
     return ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
 
@@ -41,6 +47,7 @@ class PairwiseIntegral(torch.autograd.Function):
     @staticmethod
     def forward(ctx, points, offsets, kind, max_points):
         op, p, skip = _KINDS[kind]
+        _need_cuda(points, offsets)
         points = points.contiguous()
         offsets = offsets.contiguous()
         n = offsets.numel() - 1
@@ -100,6 +107,7 @@ class _SymmetricExpand(torch.autograd.Function):
     @staticmethod
     def forward(ctx, c, n, diagonal):
         skip = nat.SKIP_LOWER if diagonal else nat.SKIP_LOWER_NODIAG
+        _need_cuda(c)
         n = int(n)
         c = c.contiguous()
         if c.numel() != int(nat.lib().sbg_output_count(skip, n, n)):
