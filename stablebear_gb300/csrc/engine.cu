@@ -1088,12 +1088,13 @@ namespace sbg
       d.q = pl.q; d.mode = mode; d.p = (T)p;
       d.rcap = rows.off[rows.n];
       d.ccap = cs.off[cs.n];
-      // The small bands at the end of the schedule take fewer rows per item
-      // (the band starts stay multiples of the row chunk), so that each
-      // still gives the planner's 6 items per SM instead of ending on a
-      // ragged last wave.  No pair's arithmetic depends on the item shape.
+      // The small bands at the end of the schedule take fewer rows per item,
+      // so that each still gives the planner's 6 items per SM instead of
+      // ending on a ragged last wave.  Only an even q is halved, so the new
+      // row chunk divides the old one and the band starts stay multiples of
+      // it.  No pair's arithmetic depends on the item shape.
       if (!direct)
-        while (d.q > 1 && problem_item_count(d) < 6ull * (uint64_t)dev.sms) d.q /= 2;
+        while (d.q % 2 == 0 && problem_item_count(d) < 6ull * (uint64_t)dev.sms) d.q /= 2;
       launch_problem<T>(d, pl, opk, bs);
       SBG_CUDA(cudaEventRecord(computed[b].e, bs));
     };

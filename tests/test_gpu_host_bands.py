@@ -40,25 +40,33 @@ def _device_pdist(pts, off):
     return out.cpu().numpy()
 
 
-def test_auto_bands_match_device_entry(capfd):
+@pytest.mark.parametrize("row_chunk", [0, 3, 12])
+def test_auto_bands_match_device_entry(capfd, row_chunk):
+    """row_chunk: rows per work item / 32 fixed by the caller (0: the
+    planner's); a band that takes fewer rows per item halves only an even
+    chunk, so 3 stays 3 and 12 may become 6 or 3."""
     import stablebear_gb300 as sb
     from stablebear_gb300 import _native as nat, synthetic
     n = 16500
     pts, off = synthetic.gaussian(n, synthetic.uniform_lengths(4, 24), np.float32, seed=21)
     assert n * (n - 1) // 2 * 4 > 512 << 20
-    want = _device_pdist(pts, off)
-    nat.lib().sbg_set_device_verbose(1)
+    sb.set_tuning(row_chunk=row_chunk)
     try:
-        got = sb.pdist(sb.PcfArray.from_csr(pts, off)).data
+        want = _device_pdist(pts, off)
+        nat.lib().sbg_set_device_verbose(1)
+        try:
+            got = sb.pdist(sb.PcfArray.from_csr(pts, off)).data
+        finally:
+            nat.lib().sbg_set_device_verbose(0)
     finally:
-        nat.lib().sbg_set_device_verbose(0)
+        sb.set_tuning()
     np.testing.assert_array_equal(got, want)
     # the phase report: one line per call, with a mark per band
     err = capfd.readouterr().err
     line = [ln for ln in err.splitlines() if ln.startswith("sbgpu host entry")]
     assert len(line) == 1
     bands = [tok for tok in line[0].split() if tok.startswith("band")]
-    assert len(bands) > 8 and "synced" in line[0] and "freed" in line[0]
+    assert len(bands) > 4 and "synced" in line[0] and "freed" in line[0]
 
 
 def test_auto_bands_cdist_match_device_entry():
